@@ -1,0 +1,182 @@
+/*
+ * uvatrmm -- FP64 triangular matrix multiply (TRMM) on one NVIDIA GB300.
+ *
+ * C ABI of libuvatrmm.so.  Plain C types only (no CUDA or torch types): a
+ * stream is passed as `void *` holding a cudaStream_t, device buffers as
+ * plain pointers.  Every `int`-returning entry point returns a
+ * uvatrmm_status; `uvatrmm_last_error()` gives the message of the calling
+ * thread's most recent failure.
+ *
+ * What each entry point replaces in the reference (uva-trasgo/UVaTRMM):
+ *   cblas_dtrmm            the MKL cblas_dtrmm the reference links
+ *                          (UVaTRMM/src/mm_triangular.c:374-387, UVaTRMM/Makefile:20)
+ *   uvatrmm_dtrmm*         the same operation with a status return, on host
+ *                          or device buffers
+ *   uvatrmm_product        the reference's per-rank product loop
+ *                          (UVaTRMM/src/mm_triangular.c:319-410) for the whole
+ *                          n x n problem, with its row mapping
+ *                          (UVaTRMM/src/mm_mapping.c:27-67, :319-366) and
+ *                          message shape (UVaTRMM/src/mm_triangular_common.c:434-511,
+ *                          :1071-1126) selecting the GPU tile schedule and tile geometry
+ *   uvatrmm_gen_*          the reference's input generator
+ *                          (UVaTRMM/src/mm_triangular_common.c:1782-1805) and seeded inputs
+ *   uvatrmm_inf_norm       matrix_rangeInfinityNorm
+ *                          (UVaTRMM/src/mm_triangular_common.c:2936-2991)
+ *   uvatrmm_map_rows       map_regular / map_balanced (UVaTRMM/src/mm_mapping.c:27-67, :319-366)
+ */
+#ifndef UVATRMM_H
+#define UVATRMM_H
+
+#include <stddef.h>
+#include <stdint.h>
+
+#ifdef __cplusplus
+extern "C" {
+#endif
+
+#if defined(_WIN32)
+#define UVATRMM_API __declspec(dllexport)
+#else
+#define UVATRMM_API __attribute__((visibility("default")))
+#endif
+
+/* ---------------------------------------------------------------- status */
+typedef enum {
+  UVATRMM_OK = 0,
+  UVATRMM_EINVAL = -1,      /* invalid argument (as the reference's INVALID_ARGS) */
+  UVATRMM_ENOMEM = -2,      /* device or pinned host allocation failed */
+  UVATRMM_EDEVICE = -3,     /* a CUDA call failed */
+  UVATRMM_ETIMEOUT = -4,    /* a kernel's bounded wait ran out; the context is still usable */
+  UVATRMM_EUNSUPPORTED = -5,/* valid but not supported (e.g. no sm_103a device) */
+  UVATRMM_EBUSY = -6,       /* serving: admission refused (HBM budget or slots) */
+  UVATRMM_ENOTREADY = -7    /* serving: request still in flight */
+} uvatrmm_status;
+
+/* ---------------------------------------------------------------- CBLAS enums */
+/* Standard CBLAS values.  Declared here unless a CBLAS header came first. */
+#if !defined(CBLAS_H) && !defined(__mkl_cblas_h__) && !defined(UVATRMM_ORACLE_MKL_SHIM_H) && \
+    !defined(CBLAS_ENUM_DEFINED_H)
+typedef enum { CblasRowMajor = 101, CblasColMajor = 102 } CBLAS_LAYOUT;
+typedef enum { CblasNoTrans = 111, CblasTrans = 112, CblasConjTrans = 113 } CBLAS_TRANSPOSE;
+typedef enum { CblasUpper = 121, CblasLower = 122 } CBLAS_UPLO;
+typedef enum { CblasNonUnit = 131, CblasUnit = 132 } CBLAS_DIAG;
+typedef enum { CblasLeft = 141, CblasRight = 142 } CBLAS_SIDE;
+#endif
+
+/* Drop-in for cblas_dtrmm (LP64): B := alpha*op(A)*B (side Left) or
+ * alpha*B*op(A) (side Right), A triangular, in place on the host buffer B.
+ * Same argument meaning as the reference's MKL call
+ * (UVaTRMM/src/mm_triangular.c:374-387).  Errors are reported like BLAS
+ * xerbla: a message on stderr and B left unchanged; the status is also
+ * available from uvatrmm_last_status(). */
+UVATRMM_API void cblas_dtrmm(CBLAS_LAYOUT layout, CBLAS_SIDE side, CBLAS_UPLO uplo, CBLAS_TRANSPOSE transa,
+                             CBLAS_DIAG diag, int M, int N, double alpha, const double *A, int lda, double *B,
+                             int ldb);
+
+/* ---------------------------------------------------------------- handle */
+typedef struct uvatrmm_handle_st *uvatrmm_handle_t;
+
+/* Creates a handle bound to the current CUDA device.  A handle owns its
+ * workspace and stream setting; use one handle per host thread. */
+UVATRMM_API int uvatrmm_create(uvatrmm_handle_t *handle);
+UVATRMM_API int uvatrmm_destroy(uvatrmm_handle_t handle);
+/* Stream (a cudaStream_t) for the handle's device work; NULL = legacy default stream. */
+UVATRMM_API int uvatrmm_set_stream(uvatrmm_handle_t handle, void *stream);
+
+/* Tuning options. */
+typedef enum {
+  UVATRMM_OPT_ENGINE = 1,   /* UVATRMM_ENGINE_*   FP64 arithmetic engine */
+  UVATRMM_OPT_SCHEDULE = 2, /* UVATRMM_SCHED_*    tile-to-SM assignment */
+  UVATRMM_OPT_SHAPE = 3,    /* UVATRMM_SHAPE_*    diagonal tile geometry */
+  UVATRMM_OPT_TILE = 4      /* 0 = automatic, 64 or 128: output tile edge */
+} uvatrmm_option;
+typedef enum { UVATRMM_ENGINE_DFMA = 0, UVATRMM_ENGINE_DMMA = 1 } uvatrmm_engine;
+/* DYNAMIC: persistent CTAs pull tiles in longest-first order.
+ * REG / BALANCED: the reference's row mappings (map_regular / map_balanced)
+ * applied to row tiles; each CTA owns one row block x one column panel. */
+typedef enum { UVATRMM_SCHED_DYNAMIC = 0, UVATRMM_SCHED_REG = 1, UVATRMM_SCHED_BALANCED = 2 } uvatrmm_schedule;
+/* TRAPEZOID: diagonal tiles skip the zero half (the reference's exact
+ * trapezoid message).  BOXES: diagonal tiles are computed as full boxes with
+ * the zero half masked (the reference's bounding-box message). */
+typedef enum { UVATRMM_SHAPE_TRAPEZOID = 0, UVATRMM_SHAPE_BOXES = 1 } uvatrmm_shape;
+UVATRMM_API int uvatrmm_set_option(uvatrmm_handle_t handle, int option, int value);
+
+/* ---------------------------------------------------------------- TRMM */
+/* Host buffers, in place on B, with status.  handle may be NULL (a
+ * per-thread default handle on the current device is used). */
+UVATRMM_API int uvatrmm_dtrmm(uvatrmm_handle_t handle, int layout, int side, int uplo, int transa, int diag,
+                              int64_t m, int64_t n, double alpha, const double *A, int64_t lda, double *B,
+                              int64_t ldb);
+
+/* Device buffers, in place on dB, ordered on the handle's stream (returns
+ * once the work is enqueued; errors from kernels surface at the next
+ * synchronising call or uvatrmm_sync). */
+UVATRMM_API int uvatrmm_dtrmm_device(uvatrmm_handle_t handle, int layout, int side, int uplo, int transa,
+                                     int diag, int64_t m, int64_t n, double alpha, const double *dA, int64_t lda,
+                                     double *dB, int64_t ldb);
+
+/* Device buffers, out of place: dC := alpha*op(A)*dB (or dB*op(A)); dB unchanged. */
+UVATRMM_API int uvatrmm_dtrmm_device_oop(uvatrmm_handle_t handle, int layout, int side, int uplo, int transa,
+                                         int diag, int64_t m, int64_t n, double alpha, const double *dA,
+                                         int64_t lda, const double *dB, int64_t ldb, double *dC, int64_t ldc);
+
+/* Waits for the handle's stream and reports any kernel-side error
+ * (UVATRMM_ETIMEOUT for an expired bounded wait). */
+UVATRMM_API int uvatrmm_sync(uvatrmm_handle_t handle);
+
+/* ---------------------------------------------------------------- reference-shaped helpers */
+/* Row block `idx` of `nblocks` over `n` rows, by the reference's mapping
+ * (schedule UVATRMM_SCHED_REG or UVATRMM_SCHED_BALANCED).  Returns
+ * UVATRMM_EINVAL where the reference aborts. */
+UVATRMM_API int uvatrmm_map_rows(int schedule, uint64_t n, uint32_t nblocks, uint32_t idx, uint64_t *begin,
+                                 uint64_t *size);
+
+/* The reference program's whole product on device buffers: C = tril(A)*B
+ * for row-major n x n A, B, C (lda = ldb = ldc = n), with the reference's
+ * mapping (reg/balanced) and message shape (boxes/trapezoid) selecting the
+ * tile schedule and diagonal-tile geometry.  Returns the GPU time of the
+ * multiply in *mult_seconds when non-NULL. */
+UVATRMM_API int uvatrmm_product(uvatrmm_handle_t handle, int64_t n, int schedule, int shape, const double *dA,
+                                const double *dB, double *dC, double *mult_seconds);
+
+/* Device input generators (bit-identical to the oracle's CPU versions).
+ * consecutive: element (i,j) of the n x n row-major matrix is
+ *   1/(((i*n + j) mod 2341) + 1), zero above the diagonal when triangular.
+ * uniform: element (i,j) of a rows x cols matrix (at d[i*rs + j*cs]) is a
+ *   seeded counter-based uniform[-1,1) value of index i*cols+j, times 2^k
+ *   with k uniform in [-spread, spread] when spread > 0; tri = 0, 'L' or 'U'
+ *   keeps one triangle (incl. diagonal) and writes `fill` elsewhere. */
+UVATRMM_API int uvatrmm_gen_consecutive(uvatrmm_handle_t handle, int64_t n, int triangular, double *d);
+UVATRMM_API int uvatrmm_gen_uniform(uvatrmm_handle_t handle, uint64_t seed, uint64_t stream, int64_t rows,
+                                    int64_t cols, double *d, int64_t rs, int64_t cs, int tri, double fill,
+                                    int spread);
+
+/* ||C||_inf of a row-major rows x cols device matrix (max row sum of |C|). */
+UVATRMM_API int uvatrmm_inf_norm(uvatrmm_handle_t handle, int64_t rows, int64_t cols, const double *dC,
+                                 int64_t ldc, double *norm);
+
+/* ---------------------------------------------------------------- measurement */
+/* Measured FP64 peak of this device in TFLOP/s for one engine
+ * (UVATRMM_ENGINE_DFMA: FMA on the CUDA cores; UVATRMM_ENGINE_DMMA: m8n8k4
+ * FP64 tensor-core MMA), from a fixed in-register workload (~30 ms).  The
+ * roofline denominator of the plain path. */
+UVATRMM_API int uvatrmm_probe_fp64_peak(uvatrmm_handle_t handle, int engine, double *tflops);
+
+/* ---------------------------------------------------------------- memory */
+/* Device memory and copies for C callers that do not include CUDA headers.
+ * kind: 1 = host to device, 2 = device to host, 3 = device to device.
+ * Copies are ordered on the handle's stream and complete before return. */
+UVATRMM_API int uvatrmm_device_alloc(size_t bytes, void **ptr);
+UVATRMM_API int uvatrmm_device_free(void *ptr);
+UVATRMM_API int uvatrmm_copy(uvatrmm_handle_t handle, void *dst, const void *src, size_t bytes, int kind);
+
+/* ---------------------------------------------------------------- errors */
+UVATRMM_API const char *uvatrmm_last_error(void);
+UVATRMM_API int uvatrmm_last_status(void);
+UVATRMM_API const char *uvatrmm_version(void);
+
+#ifdef __cplusplus
+}
+#endif
+
+#endif /* UVATRMM_H */

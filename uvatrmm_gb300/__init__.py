@@ -1,0 +1,113 @@
+"""uvatrmm_gb300: FP64 triangular matrix multiply (TRMM) on one NVIDIA GB300.
+
+The product is the C ABI of ``libuvatrmm.so`` (``include/uvatrmm.h``) and the
+``uvatrmm.x`` command line built on it.  This package only builds them and
+binds the ABI for Python callers (tests and the benchmark): every call goes
+through the CUDA library, and nothing here computes a result on the CPU.
+"""
+from __future__ import annotations
+
+import ctypes as C
+
+from ._lib import UvatrmmError, check, header_symbols, lib  # noqa: F401
+
+# CBLAS enumerations (same values as cblas.h).
+ROW, COL = 101, 102
+NOTRANS, TRANS, CONJTRANS = 111, 112, 113
+UPPER, LOWER = 121, 122
+NONUNIT, UNIT = 131, 132
+LEFT, RIGHT = 141, 142
+
+OPT_ENGINE, OPT_SCHEDULE, OPT_SHAPE, OPT_TILE = 1, 2, 3, 4
+ENGINE_DFMA, ENGINE_DMMA = 0, 1
+SCHED_DYNAMIC, SCHED_REG, SCHED_BALANCED = 0, 1, 2
+SHAPE_TRAPEZOID, SHAPE_BOXES = 0, 1
+
+OK, EINVAL, ENOMEM, EDEVICE, ETIMEOUT, EUNSUPPORTED, EBUSY, ENOTREADY = 0, -1, -2, -3, -4, -5, -6, -7
+
+
+def _ptr(x) -> int:
+    """Address of a numpy array or torch tensor."""
+    if hasattr(x, "data_ptr"):
+        return x.data_ptr()
+    return x.ctypes.data
+
+
+class Handle:
+    """Owns a uvatrmm handle on the current CUDA device."""
+
+    def __init__(self, stream=None, **options):
+        h = C.c_void_p()
+        check(lib().uvatrmm_create(C.byref(h)))
+        self.h = h
+        if stream is not None:
+            self.set_stream(stream)
+        for k, v in options.items():
+            self.set_option(k, v)
+
+    def close(self) -> None:
+        if self.h:
+            lib().uvatrmm_destroy(self.h)
+            self.h = None
+
+    def __del__(self):
+        try:
+            self.close()
+        except Exception:
+            pass
+
+    def set_stream(self, stream) -> None:
+        s = getattr(stream, "cuda_stream", stream)
+        check(lib().uvatrmm_set_stream(self.h, C.c_void_p(int(s) if s else 0)))
+
+    def set_option(self, name: str, value: int) -> None:
+        key = {"engine": OPT_ENGINE, "schedule": OPT_SCHEDULE, "shape": OPT_SHAPE, "tile": OPT_TILE}[name]
+        check(lib().uvatrmm_set_option(self.h, key, int(value)))
+
+    # -- TRMM ------------------------------------------------------------
+    def dtrmm(self, layout, side, uplo, transa, diag, m, n, alpha, A, lda, B, ldb) -> None:
+        """Host buffers (numpy float64), in place on B."""
+        check(lib().uvatrmm_dtrmm(self.h, layout, side, uplo, transa, diag, m, n, alpha,
+                                  _ptr(A), lda, _ptr(B), ldb))
+
+    def dtrmm_device(self, layout, side, uplo, transa, diag, m, n, alpha, dA, lda, dB, ldb) -> None:
+        """Device buffers (torch float64 CUDA tensors), in place on dB."""
+        check(lib().uvatrmm_dtrmm_device(self.h, layout, side, uplo, transa, diag, m, n, alpha,
+                                         _ptr(dA), lda, _ptr(dB), ldb))
+
+    def dtrmm_device_oop(self, layout, side, uplo, transa, diag, m, n, alpha, dA, lda, dB, ldb, dC, ldc) -> None:
+        check(lib().uvatrmm_dtrmm_device_oop(self.h, layout, side, uplo, transa, diag, m, n, alpha,
+                                             _ptr(dA), lda, _ptr(dB), ldb, _ptr(dC), ldc))
+
+    def sync(self) -> None:
+        check(lib().uvatrmm_sync(self.h))
+
+    def product(self, n, schedule, shape, dA, dB, dC) -> float:
+        secs = C.c_double()
+        check(lib().uvatrmm_product(self.h, n, schedule, shape, _ptr(dA), _ptr(dB), _ptr(dC), C.byref(secs)))
+        return secs.value
+
+    def probe_fp64_peak(self, engine) -> float:
+        v = C.c_double()
+        check(lib().uvatrmm_probe_fp64_peak(self.h, engine, C.byref(v)))
+        return v.value
+
+    # -- generators and norms -------------------------------------------------
+    def gen_consecutive(self, n, triangular, d) -> None:
+        check(lib().uvatrmm_gen_consecutive(self.h, n, int(triangular), _ptr(d)))
+
+    def gen_uniform(self, seed, stream, rows, cols, d, rs, cs, tri=None, fill=0.0, spread=0) -> None:
+        t = 0 if tri is None else ord(tri)
+        check(lib().uvatrmm_gen_uniform(self.h, seed, stream, rows, cols, _ptr(d), rs, cs, t, fill, spread))
+
+    def inf_norm(self, rows, cols, dC, ldc) -> float:
+        v = C.c_double()
+        check(lib().uvatrmm_inf_norm(self.h, rows, cols, _ptr(dC), ldc, C.byref(v)))
+        return v.value
+
+
+def map_rows(schedule: int, n: int, nblocks: int, idx: int):
+    """The reference's map_regular / map_balanced; None where it aborts."""
+    b, s = C.c_uint64(), C.c_uint64()
+    rc = lib().uvatrmm_map_rows(schedule, n, nblocks, idx, C.byref(b), C.byref(s))
+    return None if rc else (b.value, s.value)

@@ -1,0 +1,77 @@
+"""ctypes binding of libuvatrmm.so (the C ABI declared in include/uvatrmm.h).
+
+The library is the product: there is no Python or CPU fallback.  Loading
+fails loudly when libuvatrmm.so has not been built (``uvatrmm_gb300.build``).
+"""
+from __future__ import annotations
+
+import ctypes as C
+import os
+import re
+
+PKG = os.path.dirname(os.path.abspath(__file__))
+LIB_PATH = os.path.join(PKG, "libuvatrmm.so")
+HEADER = os.path.join(os.path.dirname(PKG), "include", "uvatrmm.h")
+
+_lib = None
+
+i32, i64, u32, u64, dbl, vp = C.c_int, C.c_int64, C.c_uint32, C.c_uint64, C.c_double, C.c_void_p
+
+# name -> (restype, argtypes)
+SIGNATURES = {
+    "cblas_dtrmm": (None, [i32, i32, i32, i32, i32, i32, i32, dbl, vp, i32, vp, i32]),
+    "uvatrmm_create": (i32, [C.POINTER(vp)]),
+    "uvatrmm_destroy": (i32, [vp]),
+    "uvatrmm_set_stream": (i32, [vp, vp]),
+    "uvatrmm_set_option": (i32, [vp, i32, i32]),
+    "uvatrmm_dtrmm": (i32, [vp, i32, i32, i32, i32, i32, i64, i64, dbl, vp, i64, vp, i64]),
+    "uvatrmm_dtrmm_device": (i32, [vp, i32, i32, i32, i32, i32, i64, i64, dbl, vp, i64, vp, i64]),
+    "uvatrmm_dtrmm_device_oop": (i32, [vp, i32, i32, i32, i32, i32, i64, i64, dbl, vp, i64, vp, i64, vp, i64]),
+    "uvatrmm_sync": (i32, [vp]),
+    "uvatrmm_map_rows": (i32, [i32, u64, u32, u32, C.POINTER(u64), C.POINTER(u64)]),
+    "uvatrmm_product": (i32, [vp, i64, i32, i32, vp, vp, vp, C.POINTER(dbl)]),
+    "uvatrmm_gen_consecutive": (i32, [vp, i64, i32, vp]),
+    "uvatrmm_gen_uniform": (i32, [vp, u64, u64, i64, i64, vp, i64, i64, i32, dbl, i32]),
+    "uvatrmm_inf_norm": (i32, [vp, i64, i64, vp, i64, C.POINTER(dbl)]),
+    "uvatrmm_probe_fp64_peak": (i32, [vp, i32, C.POINTER(dbl)]),
+    "uvatrmm_device_alloc": (i32, [C.c_size_t, C.POINTER(vp)]),
+    "uvatrmm_device_free": (i32, [vp]),
+    "uvatrmm_copy": (i32, [vp, vp, vp, C.c_size_t, i32]),
+    "uvatrmm_last_error": (C.c_char_p, []),
+    "uvatrmm_last_status": (i32, []),
+    "uvatrmm_version": (C.c_char_p, []),
+}
+
+
+class UvatrmmError(RuntimeError):
+    def __init__(self, status: int, msg: str):
+        super().__init__(f"uvatrmm status {status}: {msg}")
+        self.status = status
+
+
+def header_symbols() -> list[str]:
+    """Every function the public header declares."""
+    text = open(HEADER).read()
+    text = re.sub(r"/\*.*?\*/", "", text, flags=re.S)
+    return sorted(set(re.findall(r"UVATRMM_API\s+[\w\s\*]+?\b(\w+)\s*\(", text)))
+
+
+def lib() -> C.CDLL:
+    """Load libuvatrmm.so (raises if it is missing: there is no fallback)."""
+    global _lib
+    if _lib is None:
+        if not os.path.exists(LIB_PATH):
+            raise RuntimeError(f"{LIB_PATH} is missing: build it with `python -m uvatrmm_gb300.build`")
+        L = C.CDLL(LIB_PATH)
+        for name, (res, args) in SIGNATURES.items():
+            if hasattr(L, name):
+                f = getattr(L, name)
+                f.restype = res
+                f.argtypes = args
+        _lib = L
+    return _lib
+
+
+def check(status: int) -> None:
+    if status != 0:
+        raise UvatrmmError(status, lib().uvatrmm_last_error().decode())

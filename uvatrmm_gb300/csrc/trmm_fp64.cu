@@ -1,0 +1,545 @@
+// Plain FP64 TRMM on GB300: one persistent, warp-specialised kernel.
+//
+// The reference computes each rank's column slice as, per row block of A, a
+// cblas_dgemm over the rectangle left of the diagonal plus a cblas_dtrmm of
+// the diagonal triangle and an add (UVaTRMM/src/mm_triangular.c:319-410).
+// Here the whole product is one launch: every output tile (BM x BN) of
+// C = alpha * Lft * Rgt runs a K loop over 16-wide slabs, clipped to the
+// triangle, with dense slabs off the diagonal and masked slabs on it.
+//
+// * Staging: one producer warp issues 2-D TMA loads (cp.async.bulk.tensor)
+//   of the Lft and Rgt slabs into a STAGES-deep shared-memory ring guarded by
+//   full/empty mbarriers; K-contiguous slabs use the 128-byte swizzle so the
+//   consumers' strided reads stay (nearly) conflict-free.
+// * Compute: eight consumer warps.  Engine DFMA: each thread owns a
+//   (BM/16) x (BN/16) register tile (rows ty+16*ii, columns tx+16*jj).
+//   Engine DMMA: each warp owns a 2x4 share of the tile in m8n8k4 FP64
+//   tensor-core fragments (mma.sync ... f64).  On GB300 the FP64 pipe
+//   behind DFMA measures faster than DMMA, so DFMA is the default.
+// * Diagonal slabs: elements outside the triangle are selected to 0 (the
+//   unreferenced triangle may hold anything), the diagonal to 1 for unit
+//   diag.  Shape TRAPEZOID skips the register rows / fragments that lie
+//   entirely in the zero half (the reference's exact trapezoid message,
+//   UVaTRMM/src/mm_triangular_common.c:1071-1126); shape BOXES computes the
+//   full bounding box (UVaTRMM/src/mm_triangular_common.c:434-511).
+// * Schedule: DYNAMIC = CTAs pull tiles longest-first from an atomic counter;
+//   REG / BALANCED = each CTA owns one block of the reference's row mapping
+//   (UVaTRMM/src/mm_mapping.c:27-67, :319-366) applied to tiles, times one
+//   column panel of its column split (UVaTRMM/src/mm_triangular.c:90).
+// * Every mbarrier wait is bounded; on expiry the kernel records
+//   KERR_WAIT_TIMEOUT, drains its own copies in flight and returns.
+#include <algorithm>
+#include <cmath>
+#include <vector>
+
+#include "common.cuh"
+#include "tmap.cuh"
+#include "trmm_fp64.cuh"
+
+namespace uvt {
+namespace {
+
+constexpr int kBK = 16;
+constexpr int kMaxBlocks = 256;
+
+enum : int { SF_FIRST = 1, SF_LAST = 2 };
+
+struct StageInfo {
+  int ti, tj, kt, flags;  // ti < 0 marks the end of the work
+};
+
+struct KParams {
+  int64_t M, N, K, ldc;
+  double alpha;
+  double *C;
+  int *counter, *status;
+  int tri_left, tri_lower, unit, trapezoid;
+  int n_major, n_minor, major_rev;  // tiles along the triangular dimension / the other one
+  int sched_static, Q, CP;
+  int qb[kMaxBlocks + 1];  // work-rank bounds of the Q major blocks
+  int cb[kMaxBlocks + 1];  // bounds of the CP minor panels
+};
+
+template <int BM>
+struct Cfg {
+  static constexpr int BN = BM;
+  // Consumer warps: 8 for 64-wide tiles (2 CTAs per SM), 16 for 128-wide
+  // tiles; plus one producer warp.  Thread grid 16 (columns) x TY (rows).
+  static constexpr int NCW = BM == 128 ? 16 : 8;
+  static constexpr int THREADS = (NCW + 1) * 32;
+  static constexpr int TY = NCW * 32 / 16;
+  static constexpr int TM = BM / TY, TN = BN / 16;
+  static constexpr int STAGES = BM == 128 ? 4 : 6;
+  static constexpr int L_ELEMS = BM * kBK, R_ELEMS = BN * kBK;
+  static constexpr uint32_t STAGE_BYTES = (L_ELEMS + R_ELEMS) * 8u;
+  static constexpr int MIN_BLOCKS = BM == 128 ? 1 : 2;
+  static constexpr size_t SMEM = 1024 + STAGES * (size_t)STAGE_BYTES + STAGES * 16 + STAGES * sizeof(StageInfo);
+};
+
+// Slab element readers.  K-major slabs were written by TMA with the 128-byte
+// swizzle: element (row r, k) of a 16-double row sits in 16-byte chunk
+// (k/2) XOR (r mod 8).
+template <int BM, bool LK>
+__device__ __forceinline__ double ldL(const double *Ls, int i, int k) {
+  if constexpr (LK)
+    return Ls[i * 16 + ((((k >> 1) ^ (i & 7))) << 1) + (k & 1)];
+  else
+    return Ls[k * BM + i];
+}
+template <int BN, bool RK>
+__device__ __forceinline__ double ldR(const double *Rs, int k, int j) {
+  if constexpr (RK)
+    return Rs[j * 16 + ((((k >> 1) ^ (j & 7))) << 1) + (k & 1)];
+  else
+    return Rs[k * BN + j];
+}
+
+// Triangle test for op(A)[r, c]: returns 0 outside, 1 inside, 2 on the diagonal.
+__device__ __forceinline__ int tri_class(int64_t r, int64_t c, int lower) {
+  if (r == c) return 2;
+  return lower ? (c < r) : (c > r);
+}
+
+__device__ __forceinline__ double tri_select(double v, int cls, int unit) {
+  return cls == 0 ? 0.0 : (cls == 2 && unit ? 1.0 : v);
+}
+
+__device__ __forceinline__ void tile_kslabs(const KParams &p, int ti, int tj, int BM, int &kt0, int &kt1) {
+  int64_t kb, ke;
+  if (p.tri_left) {
+    int64_t i0 = (int64_t)ti * BM;
+    if (p.tri_lower) { kb = 0; ke = min(i0 + BM, p.K); }
+    else { kb = i0; ke = p.K; }
+  } else {
+    int64_t j0 = (int64_t)tj * BM;
+    if (p.tri_lower) { kb = j0; ke = p.K; }
+    else { kb = 0; ke = min(j0 + BM, p.K); }
+  }
+  kt0 = (int)(kb / kBK);
+  kt1 = (int)((ke + kBK - 1) / kBK);
+}
+
+__device__ __forceinline__ void decode_major(const KParams &p, int r, int minor, int &ti, int &tj) {
+  int major = p.major_rev ? (p.n_major - 1 - r) : r;
+  if (p.tri_left) { ti = major; tj = minor; }
+  else { ti = minor; tj = major; }
+}
+
+// ---------------------------------------------------------------- DFMA engine
+// Thread (tx, ty) owns rows ty + TY*ii and columns tx + 16*jj of the tile.
+template <int BM, bool LK, bool RK>
+struct DfmaEngine {
+  using C = Cfg<BM>;
+  double acc[C::TM][C::TN];
+  int tx, ty;
+
+  __device__ void init(int tid) { tx = tid & 15; ty = tid >> 4; }
+  __device__ void zero() {
+#pragma unroll
+    for (int ii = 0; ii < C::TM; ++ii)
+#pragma unroll
+      for (int jj = 0; jj < C::TN; ++jj) acc[ii][jj] = 0.0;
+  }
+  __device__ void slab(const double *Ls, const double *Rs) {
+#pragma unroll
+    for (int k = 0; k < kBK; ++k) {
+      double a[C::TM];
+#pragma unroll
+      for (int ii = 0; ii < C::TM; ++ii) a[ii] = ldL<BM, LK>(Ls, ty + C::TY * ii, k);
+#pragma unroll
+      for (int jj = 0; jj < C::TN; ++jj) {
+        const double b = ldR<C::BN, RK>(Rs, k, tx + 16 * jj);
+#pragma unroll
+        for (int ii = 0; ii < C::TM; ++ii) acc[ii][jj] = fma(a[ii], b, acc[ii][jj]);
+      }
+    }
+  }
+  // Diagonal slab `s` (k in [16s, 16s+16) of the tile's diagonal block,
+  // whose rows and columns share the same origin).
+  __device__ void slab_diag(const double *Ls, const double *Rs, int s, const KParams &p) {
+    const bool trap = p.trapezoid, lower = p.tri_lower, unit = p.unit;
+    const int c0 = 16 * s;
+#pragma unroll 1
+    for (int k = 0; k < kBK; ++k) {
+      double a[C::TM];
+      bool skip[C::TM];
+#pragma unroll
+      for (int ii = 0; ii < C::TM; ++ii) {
+        a[ii] = ldL<BM, LK>(Ls, ty + C::TY * ii, k);
+        skip[ii] = false;
+      }
+      if (p.tri_left) {
+        // op(A)[r, c0 + k] with r = ty + TY*ii; rows wholly above (lower)
+        // or below (upper) the slab lie outside the trapezoid.
+#pragma unroll
+        for (int ii = 0; ii < C::TM; ++ii) {
+          const int r = ty + C::TY * ii;
+          a[ii] = tri_select(a[ii], tri_class(r, c0 + k, lower), unit);
+          skip[ii] = trap && (lower ? (r < c0) : (r > c0 + kBK - 1));
+        }
+      }
+#pragma unroll
+      for (int jj = 0; jj < C::TN; ++jj) {
+        double b = ldR<C::BN, RK>(Rs, k, tx + 16 * jj);
+        if (!p.tri_left) {
+          // op(A)[c0 + k, c] with c = tx + 16*jj.
+          const int c = tx + 16 * jj;
+          b = tri_select(b, tri_class(c0 + k, c, lower), unit);
+          if (trap && (lower ? (c > c0 + kBK - 1) : (c < c0))) continue;
+        }
+#pragma unroll
+        for (int ii = 0; ii < C::TM; ++ii)
+          if (!skip[ii]) acc[ii][jj] = fma(a[ii], b, acc[ii][jj]);
+      }
+    }
+  }
+  __device__ void store(const KParams &p, int64_t i0, int64_t j0) {
+#pragma unroll
+    for (int jj = 0; jj < C::TN; ++jj) {
+      int64_t j = j0 + tx + 16 * jj;
+      if (j >= p.N) continue;
+#pragma unroll
+      for (int ii = 0; ii < C::TM; ++ii) {
+        int64_t i = i0 + ty + C::TY * ii;
+        if (i < p.M) p.C[i + j * p.ldc] = p.alpha * acc[ii][jj];
+      }
+    }
+  }
+};
+
+// ---------------------------------------------------------------- DMMA engine
+__device__ __forceinline__ void dmma884(double &c0, double &c1, double a, double b) {
+  asm volatile("mma.sync.aligned.m8n8k4.row.col.f64.f64.f64.f64 {%0,%1}, {%2}, {%3}, {%0,%1};"
+               : "+d"(c0), "+d"(c1)
+               : "d"(a), "d"(b));
+}
+
+template <int BM, bool LK, bool RK>
+struct DmmaEngine {
+  using C = Cfg<BM>;
+  // Warp grid (NCW/4) rows x 4 columns; warp tile WM x WN in m8n8 fragments.
+  static constexpr int WM = BM / (C::NCW / 4), WN = C::BN / 4;
+  static constexpr int FM = WM / 8, FN = WN / 8;
+  double acc[FM][FN][2];
+  int r0, c0, g, t;
+
+  __device__ void init(int tid) {
+    int w = tid >> 5, lane = tid & 31;
+    r0 = (w >> 2) * WM;
+    c0 = (w & 3) * WN;
+    g = lane >> 2;
+    t = lane & 3;
+  }
+  __device__ void zero() {
+#pragma unroll
+    for (int f = 0; f < FM; ++f)
+#pragma unroll
+      for (int h = 0; h < FN; ++h) acc[f][h][0] = acc[f][h][1] = 0.0;
+  }
+  __device__ void slab(const double *Ls, const double *Rs) {
+#pragma unroll
+    for (int k = 0; k < kBK; k += 4) {
+      double a[FM], b[FN];
+#pragma unroll
+      for (int f = 0; f < FM; ++f) a[f] = ldL<BM, LK>(Ls, r0 + 8 * f + g, k + t);
+#pragma unroll
+      for (int h = 0; h < FN; ++h) b[h] = ldR<C::BN, RK>(Rs, k + t, c0 + 8 * h + g);
+#pragma unroll
+      for (int f = 0; f < FM; ++f)
+#pragma unroll
+        for (int h = 0; h < FN; ++h) dmma884(acc[f][h][0], acc[f][h][1], a[f], b[h]);
+    }
+  }
+  __device__ void slab_diag(const double *Ls, const double *Rs, int s, const KParams &p) {
+    const bool trap = p.trapezoid, lower = p.tri_lower, unit = p.unit;
+#pragma unroll 1
+    for (int k = 0; k < kBK; k += 4) {
+      double a[FM], b[FN];
+#pragma unroll
+      for (int f = 0; f < FM; ++f) a[f] = ldL<BM, LK>(Ls, r0 + 8 * f + g, k + t);
+#pragma unroll
+      for (int h = 0; h < FN; ++h) b[h] = ldR<C::BN, RK>(Rs, k + t, c0 + 8 * h + g);
+      const int kk = 16 * s + k;  // slab-relative k of this step's first column
+      if (p.tri_left) {
+#pragma unroll
+        for (int f = 0; f < FM; ++f) a[f] = tri_select(a[f], tri_class(r0 + 8 * f + g, kk + t, lower), unit);
+#pragma unroll
+        for (int f = 0; f < FM; ++f) {
+          const int rb = r0 + 8 * f;  // fragment rows [rb, rb+8), k columns [kk, kk+4)
+          if (trap && (lower ? (kk > rb + 7) : (kk + 3 < rb))) continue;
+#pragma unroll
+          for (int h = 0; h < FN; ++h) dmma884(acc[f][h][0], acc[f][h][1], a[f], b[h]);
+        }
+      } else {
+#pragma unroll
+        for (int h = 0; h < FN; ++h) b[h] = tri_select(b[h], tri_class(kk + t, c0 + 8 * h + g, lower), unit);
+#pragma unroll
+        for (int h = 0; h < FN; ++h) {
+          const int cb = c0 + 8 * h;  // fragment columns [cb, cb+8)
+          if (trap && (lower ? (kk + 3 < cb) : (kk > cb + 7))) continue;
+#pragma unroll
+          for (int f = 0; f < FM; ++f) dmma884(acc[f][h][0], acc[f][h][1], a[f], b[h]);
+        }
+      }
+    }
+  }
+  __device__ void store(const KParams &p, int64_t i0, int64_t j0) {
+#pragma unroll
+    for (int f = 0; f < FM; ++f)
+#pragma unroll
+      for (int h = 0; h < FN; ++h) {
+        int64_t i = i0 + r0 + 8 * f + g;
+        int64_t j = j0 + c0 + 8 * h + 2 * t;
+        if (i < p.M) {
+          if (j < p.N) p.C[i + j * p.ldc] = p.alpha * acc[f][h][0];
+          if (j + 1 < p.N) p.C[i + (j + 1) * p.ldc] = p.alpha * acc[f][h][1];
+        }
+      }
+  }
+};
+
+// ---------------------------------------------------------------- kernel
+template <int BM, bool LK, bool RK, template <int, bool, bool> class EngineT>
+__global__ void __launch_bounds__(Cfg<BM>::THREADS, Cfg<BM>::MIN_BLOCKS)
+    trmm_fp64_kernel(const __grid_constant__ CUtensorMap tmL, const __grid_constant__ CUtensorMap tmR,
+                     const __grid_constant__ KParams p) {
+  using C = Cfg<BM>;
+  extern __shared__ uint8_t smem_raw[];
+  uint8_t *base = reinterpret_cast<uint8_t *>((reinterpret_cast<uintptr_t>(smem_raw) + 1023) & ~uintptr_t(1023));
+  uint64_t *full = reinterpret_cast<uint64_t *>(base + C::STAGES * C::STAGE_BYTES);
+  uint64_t *empty = full + C::STAGES;
+  StageInfo *info = reinterpret_cast<StageInfo *>(empty + C::STAGES);
+  auto Lst = [&](int s) { return reinterpret_cast<double *>(base + s * C::STAGE_BYTES); };
+  auto Rst = [&](int s) { return reinterpret_cast<double *>(base + s * C::STAGE_BYTES) + C::L_ELEMS; };
+
+  const int warp = threadIdx.x >> 5, lane = threadIdx.x & 31;
+  if (threadIdx.x == 0) {
+    for (int s = 0; s < C::STAGES; ++s) {
+      mbar_init(&full[s], 1);
+      mbar_init(&empty[s], C::NCW);
+    }
+    fence_barrier_init();
+  }
+  __syncthreads();
+
+  if (warp == C::NCW) {
+    // ------------------------------------------------------------ producer
+    if (lane == 0) {
+      tma_prefetch_desc(&tmL);
+      tma_prefetch_desc(&tmR);
+      int s = 0;
+      uint32_t ph = 0;
+      bool ok = true;
+      uint32_t issued = 0;
+      uint32_t last_ph[C::STAGES];
+      auto claim = [&]() -> bool {  // wait until stage s is free
+        if (!mbar_wait_bounded(&empty[s], ph ^ 1)) {
+          record_error(p.status, KERR_WAIT_TIMEOUT);
+          return false;
+        }
+        return true;
+      };
+      auto advance = [&]() {
+        if (++s == C::STAGES) { s = 0; ph ^= 1; }
+      };
+      auto issue_tile = [&](int ti, int tj) -> bool {
+        int kt0, kt1;
+        tile_kslabs(p, ti, tj, BM, kt0, kt1);
+        const int i0 = ti * BM, j0 = tj * C::BN;
+        for (int kt = kt0; kt < kt1; ++kt) {
+          if (!claim()) return false;
+          info[s] = StageInfo{ti, tj, kt, (kt == kt0 ? SF_FIRST : 0) | (kt == kt1 - 1 ? SF_LAST : 0)};
+          mbar_arrive_expect_tx(&full[s], C::STAGE_BYTES);
+          const int k0 = kt * kBK;
+          if constexpr (LK) tma_load_2d(Lst(s), &tmL, k0, i0, &full[s]);
+          else tma_load_2d(Lst(s), &tmL, i0, k0, &full[s]);
+          if constexpr (RK) tma_load_2d(Rst(s), &tmR, k0, j0, &full[s]);
+          else tma_load_2d(Rst(s), &tmR, j0, k0, &full[s]);
+          issued |= 1u << s;
+          last_ph[s] = ph;
+          advance();
+        }
+        return true;
+      };
+      if (!p.sched_static) {
+        const int total = p.n_major * p.n_minor;
+        while (ok) {
+          int t = atomicAdd(p.counter, 1);
+          if (t >= total) break;
+          int ti, tj;
+          decode_major(p, p.n_major - 1 - t / p.n_minor, t % p.n_minor, ti, tj);
+          ok = issue_tile(ti, tj);
+        }
+      } else if ((int)blockIdx.x < p.Q * p.CP) {
+        const int q = blockIdx.x / p.CP, c = blockIdx.x % p.CP;
+        for (int r = p.qb[q + 1] - 1; ok && r >= p.qb[q]; --r)
+          for (int m = p.cb[c]; ok && m < p.cb[c + 1]; ++m) {
+            int ti, tj;
+            decode_major(p, r, m, ti, tj);
+            ok = issue_tile(ti, tj);
+          }
+      }
+      // End-of-work marker (a plain arrive completes the phase).
+      if (claim()) {
+        info[s] = StageInfo{-1, -1, 0, 0};
+        mbar_arrive(&full[s]);
+        issued |= 1u << s;
+        last_ph[s] = ph;
+      }  // else: no stage came free; the consumers' own bounded waits end them
+      // Drain: every copy this thread issued must have landed before exit.
+      for (int st = 0; st < C::STAGES; ++st)
+        if ((issued >> st) & 1u)
+          if (!mbar_wait_bounded(&full[st], last_ph[st])) record_error(p.status, KERR_WAIT_TIMEOUT);
+    }
+  } else {
+    // ------------------------------------------------------------ consumers
+    EngineT<BM, LK, RK> eng;
+    eng.init(threadIdx.x);
+    int s = 0;
+    uint32_t ph = 0;
+    while (true) {
+      if (!mbar_wait_bounded(&full[s], ph)) {
+        record_error(p.status, KERR_WAIT_TIMEOUT);
+        break;
+      }
+      const volatile StageInfo *vi = &info[s];
+      const StageInfo inf{vi->ti, vi->tj, vi->kt, vi->flags};
+      if (inf.ti < 0) break;
+      if (inf.flags & SF_FIRST) eng.zero();
+      const int64_t i0 = (int64_t)inf.ti * BM, j0 = (int64_t)inf.tj * C::BN;
+      const int64_t k0 = (int64_t)inf.kt * kBK;
+      const int64_t d0 = p.tri_left ? i0 : j0;
+      if (k0 >= d0 && k0 < d0 + BM)
+        eng.slab_diag(Lst(s), Rst(s), (int)((k0 - d0) / kBK), p);
+      else
+        eng.slab(Lst(s), Rst(s));
+      __syncwarp();
+      if (lane == 0) mbar_arrive(&empty[s]);
+      if (inf.flags & SF_LAST) eng.store(p, i0, j0);
+      if (++s == C::STAGES) { s = 0; ph ^= 1; }
+    }
+  }
+  __syncthreads();
+}
+
+template <int BM, bool LK, bool RK, template <int, bool, bool> class EngineT>
+int launch_variant(const CUtensorMap &tmL, const CUtensorMap &tmR, const KParams &kp, int grid,
+                   cudaStream_t stream) {
+  auto kern = trmm_fp64_kernel<BM, LK, RK, EngineT>;
+  static bool attr_set = false;  // per instantiation
+  if (!attr_set) {
+    if (cudaFuncSetAttribute(kern, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)Cfg<BM>::SMEM) !=
+        cudaSuccess)
+      return UVATRMM_EDEVICE;
+    attr_set = true;
+  }
+  kern<<<grid, Cfg<BM>::THREADS, Cfg<BM>::SMEM, stream>>>(tmL, tmR, kp);
+  return cudaGetLastError() == cudaSuccess ? UVATRMM_OK : UVATRMM_EDEVICE;
+}
+
+template <int BM, template <int, bool, bool> class EngineT>
+int dispatch_layout(bool lk, bool rk, const CUtensorMap &tmL, const CUtensorMap &tmR, const KParams &kp, int grid,
+                    cudaStream_t st) {
+  if (lk && rk) return launch_variant<BM, true, true, EngineT>(tmL, tmR, kp, grid, st);
+  if (lk && !rk) return launch_variant<BM, true, false, EngineT>(tmL, tmR, kp, grid, st);
+  if (!lk && rk) return launch_variant<BM, false, true, EngineT>(tmL, tmR, kp, grid, st);
+  return launch_variant<BM, false, false, EngineT>(tmL, tmR, kp, grid, st);
+}
+
+// map_regular / map_balanced over `n` units into `P` blocks (the C restatement
+// lives beside the public uvatrmm_map_rows); fills bounds[0..P].
+int fill_bounds(int schedule, int n, int P, int *bounds) {
+  bounds[0] = 0;
+  for (int q = 0; q < P; ++q) {
+    uint64_t b, s;
+    if (uvatrmm_map_rows(schedule, (uint64_t)n, (uint32_t)P, (uint32_t)q, &b, &s) != UVATRMM_OK) return -1;
+    if ((int)b != bounds[q]) return -1;
+    bounds[q + 1] = (int)(b + s);
+  }
+  return bounds[P] == n ? 0 : -1;
+}
+
+}  // namespace
+
+int fp64_auto_tile(int64_t M, int64_t N, int64_t K, int num_sms) {
+  // The FP64 pipe, not memory, bounds this kernel on GB300, so the 64-wide
+  // tile (two CTAs per SM, no register spills) is the default everywhere;
+  // 128 stays selectable through UVATRMM_OPT_TILE.
+  (void)M; (void)N; (void)K; (void)num_sms;
+  return 64;
+}
+
+int launch_trmm_fp64(const Fp64Launch &L, cudaStream_t stream, const char **why) {
+  *why = nullptr;
+  if (L.M <= 0 || L.N <= 0 || L.K <= 0) return UVATRMM_OK;
+  const int BM = L.tile ? L.tile : fp64_auto_tile(L.M, L.N, L.K, L.num_sms);
+  if (BM != 64 && BM != 128) {
+    *why = "tile must be 0, 64 or 128";
+    return UVATRMM_EINVAL;
+  }
+  if (L.M > INT32_MAX / 2 || L.N > INT32_MAX / 2 || L.K > INT32_MAX / 2) {
+    *why = "dimension too large";
+    return UVATRMM_EINVAL;
+  }
+  CUtensorMap tmL, tmR;
+  const uint32_t boxL_in = L.lft_kmajor ? kBK : BM, boxL_out = L.lft_kmajor ? BM : kBK;
+  const uint32_t boxR_in = L.rgt_kmajor ? kBK : BM, boxR_out = L.rgt_kmajor ? BM : kBK;
+  if (make_tmap_2d(&tmL, CU_TENSOR_MAP_DATA_TYPE_FLOAT64, 8, L.xl.ptr, L.xl.rows, L.xl.cols, L.xl.ld * 8, boxL_in,
+                   boxL_out, L.lft_kmajor) ||
+      make_tmap_2d(&tmR, CU_TENSOR_MAP_DATA_TYPE_FLOAT64, 8, L.xr.ptr, L.xr.rows, L.xr.cols, L.xr.ld * 8, boxR_in,
+                   boxR_out, L.rgt_kmajor)) {
+    *why = "tensor map encoding failed (alignment or driver)";
+    return UVATRMM_EDEVICE;
+  }
+
+  KParams kp;
+  memset(&kp, 0, sizeof(kp));
+  kp.M = L.M; kp.N = L.N; kp.K = L.K; kp.ldc = L.ldc;
+  kp.alpha = L.alpha; kp.C = L.C; kp.counter = L.counter; kp.status = L.status;
+  kp.tri_left = L.tri_left; kp.tri_lower = L.tri_lower; kp.unit = L.unit;
+  kp.trapezoid = L.shape == UVATRMM_SHAPE_TRAPEZOID;
+  const int tiles_m = (int)((L.M + BM - 1) / BM), tiles_n = (int)((L.N + BM - 1) / BM);
+  kp.n_major = L.tri_left ? tiles_m : tiles_n;
+  kp.n_minor = L.tri_left ? tiles_n : tiles_m;
+  // Work grows with the major index for (left, lower) and (right, upper).
+  const bool grows = L.tri_left ? L.tri_lower : !L.tri_lower;
+  kp.major_rev = grows ? 0 : 1;
+
+  const int per_sm = BM == 128 ? Cfg<128>::MIN_BLOCKS : Cfg<64>::MIN_BLOCKS;
+  int grid;
+  if (L.schedule == UVATRMM_SCHED_DYNAMIC) {
+    grid = std::min<int64_t>((int64_t)L.num_sms * per_sm, (int64_t)tiles_m * tiles_n);
+    if (cudaMemsetAsync(L.counter, 0, sizeof(int), stream) != cudaSuccess) return UVATRMM_EDEVICE;
+  } else {
+    // Q row blocks (reference mapping over the major tiles) x CP column
+    // panels (map_regular over the minor tiles), Q*CP <= CTAs resident.
+    const int slots = L.num_sms * per_sm;
+    int CP = 1;
+    while (CP * 2 <= kp.n_minor && slots / (CP * 2) >= 2 && kp.n_minor % (CP * 2) == 0 &&
+           slots / (CP * 2) >= kp.n_major / 8)
+      CP *= 2;
+    int Q = std::min(std::min(slots / CP, kp.n_major), kMaxBlocks);
+    CP = std::min(CP, kMaxBlocks);
+    // Shrink Q until the reference mapping accepts it (it aborts when a
+    // block would be empty).
+    while (Q > 1 && fill_bounds(L.schedule, kp.n_major, Q, kp.qb) != 0) --Q;
+    if (fill_bounds(L.schedule, kp.n_major, Q, kp.qb) != 0 ||
+        fill_bounds(UVATRMM_SCHED_REG, kp.n_minor, CP, kp.cb) != 0) {
+      *why = "row mapping rejected the tile counts";
+      return UVATRMM_EINVAL;
+    }
+    kp.sched_static = 1;
+    kp.Q = Q;
+    kp.CP = CP;
+    grid = Q * CP;
+  }
+  const bool lk = L.lft_kmajor, rk = L.rgt_kmajor;
+  if (L.engine == UVATRMM_ENGINE_DMMA) {
+    if (BM == 128) return dispatch_layout<128, DmmaEngine>(lk, rk, tmL, tmR, kp, grid, stream);
+    return dispatch_layout<64, DmmaEngine>(lk, rk, tmL, tmR, kp, grid, stream);
+  }
+  if (BM == 128) return dispatch_layout<128, DfmaEngine>(lk, rk, tmL, tmR, kp, grid, stream);
+  return dispatch_layout<64, DfmaEngine>(lk, rk, tmL, tmR, kp, grid, stream);
+}
+
+}  // namespace uvt
