@@ -10,16 +10,16 @@ namespace uvt {
 namespace {
 
 __global__ void __launch_bounds__(256) probe_dfma(double *out, double seed, int iters) {
-  double x[8];
+  double x[16];
 #pragma unroll
-  for (int i = 0; i < 8; ++i) x[i] = seed + threadIdx.x * 1e-9 + i;
+  for (int i = 0; i < 16; ++i) x[i] = seed + threadIdx.x * 1e-9 + i;
   const double m = 0.999999, c = 1e-7;
   for (int it = 0; it < iters; ++it)
 #pragma unroll
-    for (int i = 0; i < 8; ++i) x[i] = fma(x[i], m, c);
+    for (int i = 0; i < 16; ++i) x[i] = fma(x[i], m, c);
   double s = 0;
 #pragma unroll
-  for (int i = 0; i < 8; ++i) s += x[i];
+  for (int i = 0; i < 16; ++i) s += x[i];
   out[blockIdx.x * blockDim.x + threadIdx.x] = s;
 }
 
@@ -53,9 +53,11 @@ extern "C" UVATRMM_API int uvatrmm_probe_fp64_peak(uvatrmm_handle_t h, int engin
   const int blocks = h->num_sms * 8, threads = 256;
   double *out = static_cast<double *>(workspace(h, 3, (size_t)blocks * threads * 8));
   if (!out) return uvatrmm_last_status();
-  // flops per thread per iteration: DFMA 8 chains x 2; DMMA 4 x (8*8*4*2)/32.
-  const double fpt = engine == UVATRMM_ENGINE_DFMA ? 16.0 : 64.0;
-  const int iters = engine == UVATRMM_ENGINE_DFMA ? 4000 : 1000;
+  // flops per thread per iteration: DFMA 16 chains x 2; DMMA 4 x (8*8*4*2)/32.
+  // About 100 ms per launch at GB300's FP64 rate, best of three after a
+  // warm-up launch, so the clocks have settled.
+  const double fpt = engine == UVATRMM_ENGINE_DFMA ? 32.0 : 64.0;
+  const int iters = engine == UVATRMM_ENGINE_DFMA ? 12000 : 6000;
   auto launch = [&](int it) {
     if (engine == UVATRMM_ENGINE_DFMA) probe_dfma<<<blocks, threads, 0, h->stream>>>(out, 1.0, it);
     else probe_dmma<<<blocks, threads, 0, h->stream>>>(out, 1.0, it);
