@@ -37,6 +37,10 @@ sys.path.insert(0, ROOT)
 
 METRIC = "TRMM TFLOP/s, FP64 DMMA vs Ozaki at <=1e-14 rel err; served p50/p99 latency"
 NOMINAL_FP64_TFLOPS = 1.25
+FP64_FLOP_PER_CLK_SM = 4.0
+# DRAM bytes per flop of the FP64 kernel measured by ncu at m = n = 4096
+# (1.2965e9 B over 4096^3 flops); B panels are re-read per row tile.
+TRAFFIC_BYTES_PER_FLOP = 1.2965e9 / 4096.0 ** 3
 
 
 def dist_env():
@@ -178,7 +182,11 @@ def run_gpu(args, ws, rank, local):
     flops = float(m) * m * n
     value = ws * flops * args.steps / (total_ms * 1e-3) / 1e12
     achieved = flops / (statistics.mean(per_launch) * 1e-3) / 1e12
-    peak = max(peak_dfma, peak_dmma)
+    clocks = clk.summary()
+    sm_mhz = clocks.get("sm_mhz") or 2070.0
+    n_sms = torch.cuda.get_device_properties(dev).multi_processor_count
+    # FP64 issue limit: 2 DFMA (4 flop) per clock per SM at the sampled clock.
+    peak = FP64_FLOP_PER_CLK_SM * n_sms * sm_mhz * 1e6 / 1e12
 
     # correctness spot check of the timed output: 4 sampled columns vs OpenBLAS (rank 0 only)
     relerr = None
@@ -226,12 +234,17 @@ def run_gpu(args, ws, rank, local):
                 "d2h_bytes_per_step": 8 * m * n, "api": "uvatrmm_dtrmm (host pointers, pinned)",
                 "steps": e2e_steps},
         "roofline": {"bound": "tensor", "achieved": round(achieved, 4), "peak": round(peak, 4), "unit": "TFLOP/s",
-                     "frac": round(achieved / peak, 4), "traffic": None,
-                     "peak_source": f"measured in this run by uvatrmm_probe_fp64_peak: DFMA {peak_dfma:.3f}, "
-                                    f"DMMA {peak_dmma:.3f} TFLOP/s (nominal GB300 FP64 {NOMINAL_FP64_TFLOPS})",
-                     "frac_of_dmma_peak": round(achieved / peak_dmma, 4)},
+                     "frac": round(achieved / peak, 4),
+                     "traffic": TRAFFIC_BYTES_PER_FLOP * flops if m == n else None,
+                     "peak_source": f"FP64 issue limit {FP64_FLOP_PER_CLK_SM} flop/clk/SM x {n_sms} SMs x "
+                                    f"{sm_mhz:.0f} MHz (sampled); MEASURED_PEAKS.json has no FP64 figure; "
+                                    f"in-run probe kernels: DFMA {peak_dfma:.3f}, DMMA {peak_dmma:.3f} TFLOP/s; "
+                                    f"nominal GB300 FP64 {NOMINAL_FP64_TFLOPS}",
+                     "frac_of_nominal": round(achieved / NOMINAL_FP64_TFLOPS, 4),
+                     "traffic_source": "dram bytes per launch scaled by flops from the m=4096 ncu capture "
+                                       "(profiles/trmm_fp64_dfma_m16384.md)"},
         "gpu_launches": args.steps,
-        "clocks": clk.summary(),
+        "clocks": clocks,
         "check": {"sampled_rel_fro_err_vs_openblas": relerr},
     }
     return out

@@ -88,7 +88,8 @@ typedef enum {
   UVATRMM_OPT_ENGINE = 1,   /* UVATRMM_ENGINE_*   FP64 arithmetic engine */
   UVATRMM_OPT_SCHEDULE = 2, /* UVATRMM_SCHED_*    tile-to-SM assignment */
   UVATRMM_OPT_SHAPE = 3,    /* UVATRMM_SHAPE_*    diagonal tile geometry */
-  UVATRMM_OPT_TILE = 4      /* 0 = automatic, 64 or 128: output tile edge */
+  UVATRMM_OPT_TILE = 4,     /* 0 = automatic, 64 or 128: output tile edge */
+  UVATRMM_OPT_OZAKI_SCRATCH_MB = 5 /* Ozaki residue-plane budget per pass, MiB (default 49152) */
 } uvatrmm_option;
 typedef enum { UVATRMM_ENGINE_DFMA = 0, UVATRMM_ENGINE_DMMA = 1 } uvatrmm_engine;
 /* DYNAMIC: persistent CTAs pull tiles in longest-first order.
@@ -119,6 +120,27 @@ UVATRMM_API int uvatrmm_dtrmm_device(uvatrmm_handle_t handle, int layout, int si
 UVATRMM_API int uvatrmm_dtrmm_device_oop(uvatrmm_handle_t handle, int layout, int side, int uplo, int transa,
                                          int diag, int64_t m, int64_t n, double alpha, const double *dA,
                                          int64_t lda, const double *dB, int64_t ldb, double *dC, int64_t ldc);
+
+/* ---------------------------------------------------------------- Ozaki (emulated FP64) */
+/* The same TRMM computed exactly in integer arithmetic on the bf16 tensor
+ * cores and rounded once to FP64 (Ozaki-style splitting with `moduli`
+ * residue slices; 0 = automatic, 2..20).  Same arguments and in-place
+ * semantics as uvatrmm_dtrmm_device / uvatrmm_dtrmm; there is no reference
+ * counterpart (the reference runs FP64 MKL only).  When relerr_out is not
+ * NULL it receives the relative Frobenius error of the result against the
+ * plain FP64 kernel over 8 evenly spaced result columns (side Left) or rows
+ * (side Right), and the call synchronises.  *bits_out (if not NULL) receives
+ * the bits kept per scaled operand entry. */
+UVATRMM_API int uvatrmm_ozaki_dtrmm_device(uvatrmm_handle_t handle, int layout, int side, int uplo, int transa,
+                                          int diag, int64_t m, int64_t n, double alpha, const double *dA,
+                                          int64_t lda, double *dB, int64_t ldb, int moduli, double *relerr_out,
+                                          int *bits_out);
+UVATRMM_API int uvatrmm_ozaki_dtrmm(uvatrmm_handle_t handle, int layout, int side, int uplo, int transa, int diag,
+                                   int64_t m, int64_t n, double alpha, const double *A, int64_t lda, double *B,
+                                   int64_t ldb, int moduli, double *relerr_out, int *bits_out);
+/* Residue slices the automatic choice uses for inner dimension k, and the
+ * bits per scaled entry that `moduli` slices give for it. */
+UVATRMM_API int uvatrmm_ozaki_plan(int64_t k, int moduli, int *moduli_out, int *bits_out);
 
 /* Waits for the handle's stream and reports any kernel-side error
  * (UVATRMM_ETIMEOUT for an expired bounded wait). */

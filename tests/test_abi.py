@@ -79,3 +79,15 @@ def test_no_gpu_reports_device_error(built):
     h = C.c_void_p()
     rc = u.lib().uvatrmm_create(C.byref(h))
     assert rc in (u.EDEVICE, u.EUNSUPPORTED)
+
+
+def test_ozaki_plan_is_monotonic(built):
+    prev = 0
+    for mo in range(2, 21):
+        n, bits = u.ozaki_plan(4096, mo)
+        assert n == mo and bits >= prev
+        prev = bits
+    auto, bits = u.ozaki_plan(32768)
+    assert bits >= 56 and 14 <= auto <= 20
+    with pytest.raises(u.UvatrmmError):
+        u.ozaki_plan(100, 1)

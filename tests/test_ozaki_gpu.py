@@ -1,0 +1,136 @@
+"""Ozaki-style emulated FP64 TRMM on the GPU, through the C ABI.
+
+Bars: bit-exact where the exact product is representable (integer inputs);
+relative Frobenius error <= 1e-14 against the oracle's double-double TRMM
+otherwise (the spec accuracy target).
+"""
+import itertools
+
+import numpy as np
+import pytest
+
+import uvatrmm_gb300 as u
+from oracle import oracle as orc
+from tests.helpers import (COL, LEFT, LOWER, NONUNIT, NOTRANS, RIGHT, ROW, TRANS, UNIT, UPPER, make_problem,
+                           rel_fro)
+
+pytestmark = pytest.mark.gpu
+VARIANTS = list(itertools.product((COL, ROW), (LEFT, RIGHT), (LOWER, UPPER), (NOTRANS, TRANS), (NONUNIT, UNIT)))
+TOL = 1e-14
+
+
+def dd_reference(layout, side, uplo, trans, diag, m, n, alpha, A, lda, B, ldb):
+    """Double-double result written back into a copy of B's storage."""
+    ref_cm = orc.dtrmm_dd(layout, side, uplo, trans, diag, m, n, alpha, A, lda, B, ldb)
+    out = B.copy()
+    M, N = ref_cm.shape
+    for j in range(N):
+        out[j * ldb:j * ldb + M] = ref_cm[:, j]
+    return out
+
+
+@pytest.mark.parametrize("layout,side,uplo,trans,diag", VARIANTS)
+def test_ozaki_all_variants_vs_double_double(handle, layout, side, uplo, trans, diag):
+    m, n = 70, 90
+    A, lda, B, ldb = make_problem(layout, side, uplo, m, n, lda_pad=1, ldb_pad=2)
+    ref = dd_reference(layout, side, uplo, trans, diag, m, n, -0.5, A, lda, B, ldb)
+    got = B.copy()
+    err, bits = handle.ozaki(layout, side, uplo, trans, diag, m, n, -0.5, A, lda, got, ldb, want_err=True)
+    pad = B == -7.0
+    assert np.array_equal(got[pad], B[pad])
+    assert rel_fro(got[~pad], ref[~pad]) <= TOL
+    assert bits >= 56 and err <= TOL
+
+
+@pytest.mark.parametrize("K", [513, 1100, 2500])
+@pytest.mark.parametrize("side", [LEFT, RIGHT])
+def test_ozaki_exact_on_integer_inputs(handle, K, side):
+    """Integer operands: the emulated product is exact, across several
+    512-wide K chunks (exercising the in-TMEM modular folds)."""
+    rng = np.random.default_rng(K)
+    m, n = (K, 37) if side == LEFT else (37, K)
+    Af = rng.integers(-1024, 1025, size=(K, K)).astype(np.float64)
+    Bf = rng.integers(-1024, 1025, size=(m, n)).astype(np.float64)
+    exact = (np.tril(Af).astype(np.int64) @ Bf.astype(np.int64)) if side == LEFT else \
+        (Bf.astype(np.int64) @ np.tril(Af).astype(np.int64))
+    A = np.asfortranarray(Af).ravel(order="F").copy()
+    B = np.asfortranarray(Bf).ravel(order="F").copy()
+    handle.ozaki(COL, side, LOWER, NOTRANS, NONUNIT, m, n, 1.0, A, K, B, m)
+    got = B.reshape(n, m).T
+    assert np.array_equal(got, exact.astype(np.float64))
+
+
+def test_ozaki_device_in_place_matches_host(handle):
+    import torch
+    m, n = 300, 200
+    A, lda, B, ldb = make_problem(COL, LEFT, UPPER, m, n)
+    host = B.copy()
+    handle.ozaki(COL, LEFT, UPPER, TRANS, NONUNIT, m, n, 1.0, A, lda, host, ldb)
+    dA = torch.from_numpy(A).cuda()
+    dB = torch.from_numpy(B.copy()).cuda()
+    handle.ozaki_device(COL, LEFT, UPPER, TRANS, NONUNIT, m, n, 1.0, dA, lda, dB, ldb)
+    handle.sync()
+    assert np.array_equal(dB.cpu().numpy(), host)
+
+
+def test_ozaki_passes_do_not_change_the_result(handle):
+    m, n = 640, 300
+    A, lda, B, ldb = make_problem(COL, RIGHT, LOWER, m, n)
+    one = B.copy()
+    handle.ozaki(COL, RIGHT, LOWER, NOTRANS, NONUNIT, m, n, 1.0, A, lda, one, ldb, moduli=16)
+    handle.set_option("tile", 0)
+    try:
+        u.check(u.lib().uvatrmm_set_option(handle.h, 5, 64))  # 64 MiB of residue planes per pass
+        many = B.copy()
+        handle.ozaki(COL, RIGHT, LOWER, NOTRANS, NONUNIT, m, n, 1.0, A, lda, many, ldb, moduli=16)
+    finally:
+        u.check(u.lib().uvatrmm_set_option(handle.h, 5, 49152))
+    assert np.array_equal(one, many)
+
+
+def test_ozaki_wide_exponent_sweep(handle):
+    """Entries uniform[-1,1) * 2^k, k in [-20, 20] (the precision config's
+    distribution): error falls with the slice count and meets 1e-14 with the
+    automatic choice."""
+    m = n = 384
+    Am = orc.fill_wide(2, 0, m, m, spread=20)
+    Bm = orc.fill_wide(2, 1, m, n, spread=20)
+    A = np.asfortranarray(np.triu(Am)).ravel(order="F").copy()
+    B = np.asfortranarray(Bm).ravel(order="F").copy()
+    ref = orc.dtrmm_dd(COL, LEFT, UPPER, TRANS, NONUNIT, m, n, 1.0, A, m, B, m)
+    errs = {}
+    for mo in (10, 12, 14, 16, 18, 20):
+        got = B.copy()
+        est, bits = handle.ozaki(COL, LEFT, UPPER, TRANS, NONUNIT, m, n, 1.0, A, m, got, m, moduli=mo,
+                                 want_err=True)
+        errs[mo] = rel_fro(got.reshape(n, m).T, ref)
+    assert errs[20] <= errs[10]
+    got = B.copy()
+    handle.ozaki(COL, LEFT, UPPER, TRANS, NONUNIT, m, n, 1.0, A, m, got, m)
+    assert rel_fro(got.reshape(n, m).T, ref) <= TOL, errs
+
+
+@pytest.mark.parametrize("m,n", [(0, 4), (4, 0), (1, 1), (1, 300), (300, 1), (129, 257)])
+def test_ozaki_edge_sizes(handle, m, n):
+    for side in (LEFT, RIGHT):
+        A, lda, B, ldb = make_problem(COL, side, LOWER, m, n)
+        ref = dd_reference(COL, side, LOWER, NOTRANS, UNIT, m, n, 3.0, A, lda, B, ldb) if m and n else B.copy()
+        got = B.copy()
+        handle.ozaki(COL, side, LOWER, NOTRANS, UNIT, m, n, 3.0, A, lda, got, ldb)
+        pad = B == -7.0
+        assert rel_fro(got[~pad], ref[~pad]) <= TOL
+
+
+def test_ozaki_zero_rows_and_alpha_zero(handle):
+    m, n = 50, 40
+    A, lda, B, ldb = make_problem(COL, LEFT, LOWER, m, n)
+    B2 = B.copy()
+    B2[5 * ldb:6 * ldb - 2] = 0.0  # one zero column of B
+    ref = dd_reference(COL, LEFT, LOWER, NOTRANS, NONUNIT, m, n, 1.0, A, lda, B2, ldb)
+    got = B2.copy()
+    handle.ozaki(COL, LEFT, LOWER, NOTRANS, NONUNIT, m, n, 1.0, A, lda, got, ldb)
+    assert np.all(got[5 * ldb:5 * ldb + m] == 0.0)
+    assert rel_fro(got, ref) <= TOL
+    got = B.copy()
+    handle.ozaki(COL, LEFT, LOWER, NOTRANS, NONUNIT, m, n, 0.0, A, lda, got, ldb)
+    assert np.all(got.reshape(n, ldb)[:, :m] == 0.0)

@@ -82,6 +82,24 @@ class Handle:
     def sync(self) -> None:
         check(lib().uvatrmm_sync(self.h))
 
+    # -- Ozaki (emulated FP64) --------------------------------------------------
+    def ozaki_device(self, layout, side, uplo, transa, diag, m, n, alpha, dA, lda, dB, ldb, moduli=0,
+                     want_err=False):
+        """Device buffers, in place on dB.  Returns (relerr or None, bits)."""
+        err, bits = C.c_double(), C.c_int()
+        check(lib().uvatrmm_ozaki_dtrmm_device(self.h, layout, side, uplo, transa, diag, m, n, alpha,
+                                               _ptr(dA), lda, _ptr(dB), ldb, moduli,
+                                               C.byref(err) if want_err else None, C.byref(bits)))
+        return (err.value if want_err else None), bits.value
+
+    def ozaki(self, layout, side, uplo, transa, diag, m, n, alpha, A, lda, B, ldb, moduli=0, want_err=False):
+        """Host buffers, in place on B.  Returns (relerr or None, bits)."""
+        err, bits = C.c_double(), C.c_int()
+        check(lib().uvatrmm_ozaki_dtrmm(self.h, layout, side, uplo, transa, diag, m, n, alpha,
+                                        _ptr(A), lda, _ptr(B), ldb, moduli,
+                                        C.byref(err) if want_err else None, C.byref(bits)))
+        return (err.value if want_err else None), bits.value
+
     def product(self, n, schedule, shape, dA, dB, dC) -> float:
         secs = C.c_double()
         check(lib().uvatrmm_product(self.h, n, schedule, shape, _ptr(dA), _ptr(dB), _ptr(dC), C.byref(secs)))
@@ -104,6 +122,13 @@ class Handle:
         v = C.c_double()
         check(lib().uvatrmm_inf_norm(self.h, rows, cols, _ptr(dC), ldc, C.byref(v)))
         return v.value
+
+
+def ozaki_plan(k: int, moduli: int = 0):
+    """(moduli, bits per scaled entry) the Ozaki path uses for inner dimension k."""
+    mo, bi = C.c_int(), C.c_int()
+    check(lib().uvatrmm_ozaki_plan(k, moduli, C.byref(mo), C.byref(bi)))
+    return mo.value, bi.value
 
 
 def map_rows(schedule: int, n: int, nblocks: int, idx: int):

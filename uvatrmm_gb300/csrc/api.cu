@@ -81,14 +81,6 @@ int collect_status(uvatrmm_handle_t h) {
 
 // ------------------------------------------------------------------ TRMM core
 
-namespace {
-
-struct Trmm {
-  int side, uplo, trans, unit;  // column-major normalised
-  int64_t m, n;                 // B is m x n
-  double alpha;
-};
-
 // Argument checks in the order (and with the parameter numbers) of the
 // reference BLAS cblas_dtrmm; returns 0 or the 1-based index of the first
 // bad argument (as xerbla reports it).
@@ -127,6 +119,8 @@ Trmm normalise(int layout, int side, int uplo, int transa, int diag, int64_t m, 
   t.alpha = alpha;
   return t;
 }
+
+namespace {
 
 bool tma_ok(const void *p, int64_t ld) { return (reinterpret_cast<uintptr_t>(p) % 16 == 0) && (ld % 2 == 0); }
 
@@ -177,6 +171,8 @@ int zero_device(uvatrmm_handle_t h, double *dB, int64_t ldb, int64_t rows, int64
   return e == cudaSuccess ? UVATRMM_OK : cuda_fail(e, "zero fill");
 }
 
+}  // namespace
+
 // Device-side core shared by the in-place and out-of-place entry points.
 // dC receives the result (may equal dB only when `in_place`).
 int device_trmm(uvatrmm_handle_t h, int layout, int side, int uplo, int transa, int diag, int64_t m, int64_t n,
@@ -216,7 +212,6 @@ int device_trmm(uvatrmm_handle_t h, int layout, int side, int uplo, int transa, 
   return rc == UVATRMM_OK ? ok() : rc;
 }
 
-}  // namespace
 }  // namespace uvt
 
 using namespace uvt;
@@ -256,7 +251,7 @@ UVATRMM_API int uvatrmm_create(uvatrmm_handle_t *handle) {
 UVATRMM_API int uvatrmm_destroy(uvatrmm_handle_t h) {
   if (!h) return ok();
   cudaStreamSynchronize(h->stream);
-  for (int i = 0; i < 4; ++i)
+  for (int i = 0; i < uvatrmm_handle_st::kSlots; ++i)
     if (h->ws[i]) cudaFree(h->ws[i]);
   if (h->dctl) cudaFree(h->dctl);
   if (h->ev0) cudaEventDestroy(h->ev0);
@@ -291,6 +286,10 @@ UVATRMM_API int uvatrmm_set_option(uvatrmm_handle_t h, int option, int value) {
     case UVATRMM_OPT_TILE:
       if (value != 0 && value != 64 && value != 128) break;
       h->tile = value;
+      return ok();
+    case UVATRMM_OPT_OZAKI_SCRATCH_MB:
+      if (value < 64) break;
+      h->ozaki_scratch_mb = value;
       return ok();
     default:
       return fail(UVATRMM_EINVAL, "unknown option");

@@ -17,9 +17,13 @@ struct uvatrmm_handle_st {
   int schedule = UVATRMM_SCHED_DYNAMIC;
   int shape = UVATRMM_SHAPE_TRAPEZOID;
   int tile = 0;
-  // Grow-only device workspace slots.
-  void *ws[4] = {nullptr, nullptr, nullptr, nullptr};
-  size_t ws_cap[4] = {0, 0, 0, 0};
+  int64_t ozaki_scratch_mb = 49152;  // residue-plane budget per pass (MiB)
+  // Grow-only device workspace slots: 0-2 plain-path staging, 3 reductions,
+  // 4 Ozaki scales, 5 Ozaki residue planes, 6 Ozaki product residues,
+  // 7 Ozaki error-estimate scratch.
+  static constexpr int kSlots = 8;
+  void *ws[kSlots] = {};
+  size_t ws_cap[kSlots] = {};
   int *dctl = nullptr;  // [0] tile counter, [1] kernel status word
   cudaEvent_t ev0 = nullptr, ev1 = nullptr;
   std::mutex mu;
@@ -43,5 +47,26 @@ void *workspace(uvatrmm_handle_t h, int slot, size_t bytes);
 int collect_status(uvatrmm_handle_t h);
 
 inline int64_t round_up(int64_t x, int64_t m) { return (x + m - 1) / m * m; }
+
+// Column-major normalised TRMM description (CBLAS row-major calls are
+// turned into the column-major call on the transposed matrices).
+struct Trmm {
+  int side, uplo, trans, unit;  // CBLAS enum values; trans/unit as 0/1
+  int64_t m, n;                 // B is m x n
+  double alpha;
+};
+int check_args(int layout, int side, int uplo, int transa, int diag, int64_t m, int64_t n, int64_t lda,
+               int64_t ldb);
+Trmm normalise(int layout, int side, int uplo, int transa, int diag, int64_t m, int64_t n, double alpha);
+
+// Plain FP64 TRMM on device buffers (stages misaligned operands, and B when
+// in place, through workspace slots 0 and 1).
+int device_trmm(uvatrmm_handle_t h, int layout, int side, int uplo, int transa, int diag, int64_t m, int64_t n,
+                double alpha, const double *dA, int64_t lda, const double *dB, int64_t ldb, double *dC,
+                int64_t ldc, bool in_place, int schedule, int shape);
+
+// ||X - R||_F / ||R||_F over column-major device blocks.
+int rel_frobenius(uvatrmm_handle_t h, int64_t rows, int64_t cols, const double *X, int64_t ldx, const double *R,
+                  int64_t ldr, double *rel);
 
 }  // namespace uvt

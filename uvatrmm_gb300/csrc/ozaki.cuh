@@ -1,0 +1,85 @@
+// Ozaki-style split-precision FP64 TRMM on GB300's bf16 tensor cores.
+//
+// The emulated product C = alpha * Lft * Rgt (the same canonical GEMM view as
+// the plain path, one operand triangular) is computed exactly in integers and
+// rounded once:
+//   1. scaling  - each row p of Lft and column p of Rgt gets a power-of-two
+//      scale so its entries become integers of at most t bits
+//      (Lft'[i,k] = rint(Lft[i,k] * 2^(t - e_i)), likewise Rgt');
+//   2. slicing  - every integer is cut into its residues modulo N pairwise
+//      coprime moduli m_l <= 256; each residue, balanced into [-128, 128],
+//      is exactly representable in bf16;
+//   3. products - for every modulus, one bf16 x bf16 -> fp32 tcgen05 GEMM of
+//      the residue matrices.  Products are < 2^14 and every K chunk of 512 is
+//      reduced modulo m_l in the fp32 accumulator (in TMEM) before the next,
+//      so every accumulated value stays below 2^24 and the accumulation is
+//      exact: the kernel yields C' mod m_l exactly;
+//   4. reassembly - the Chinese remainder theorem rebuilds C' (|C'| < M/2,
+//      M = prod m_l, up to 192 bits) per element, which is rounded once to
+//      FP64 and scaled back by 2^(e_i + d_j - 2t) * alpha.
+// N (the slice count) sets M and hence t; see ozaki_bits().
+#pragma once
+
+#include <cuda_runtime.h>
+#include <stdint.h>
+
+namespace uvt {
+
+constexpr int kMaxModuli = 20;
+// Pairwise coprime, largest first: 2^8, 3*5*17, 11*23, 251, 13*19, 241, 239,
+// 233, 229, 227, 223, 7*31, 211, 199, 197, 193, 191, 181, 179, 173.
+constexpr int kModuli[kMaxModuli] = {256, 255, 253, 251, 247, 241, 239, 233, 229, 227,
+                                     223, 217, 211, 199, 197, 193, 191, 181, 179, 173};
+
+// Bits t kept per scaled operand entry for n moduli and inner dimension K:
+// the largest t with K * 2^(2t) < M / 4.
+int ozaki_bits(int n_moduli, int64_t K);
+// Slice count the automatic choice uses for inner dimension K (t >= 56).
+int ozaki_auto_moduli(int64_t K);
+
+// One operand of the emulated product as the residue kernels see it:
+// P[p, k] = kcontig ? X[k + p*ld] : X[p + k*ld], p < P, k < K.
+// `tri` = 0: dense; 1: this operand is op(A); then the triangle test uses
+// (r, c) = p_is_row ? (p, k) : (k, p).
+struct OzOperand {
+  const double *X;
+  int64_t ld;
+  int64_t P, K;
+  bool kcontig;
+  bool tri, p_is_row, lower, unit;
+};
+
+struct OzPlan {
+  int n_moduli;       // N
+  int bits;           // t
+  int64_t M, N, K;    // canonical GEMM sizes
+  int64_t Mp, Np, Kp; // padded: Mp % 128 == 0, Np % 256 == 0, Kp % 64 == 0
+};
+
+// Device pieces (ozaki_prep.cu).
+// Row/column exponents: e[p] = max over valid k of (ilogb|P[p,k]| + 1).
+int oz_scales(const OzOperand &op, int *e, cudaStream_t st);
+// Residues of moduli [l0, l1) as bf16 planes R[l - l0][p][k] (p < Pp, k < Kp).
+int oz_residues(const OzOperand &op, const int *e, int bits, int l0, int l1, int64_t Pp, int64_t Kp, uint16_t *R,
+                cudaStream_t st);
+// CRT reassembly of C (column-major, ldc) from residue planes
+// res[l][j][i] (uint8, plane stride Mp*Np, ld Mp).
+int oz_reassemble(const OzPlan &plan, const uint8_t *res, const int *e_row, const int *e_col, double alpha,
+                  double *C, int64_t ldc, cudaStream_t st);
+
+// The tcgen05 residue GEMM (ozaki_gemm.cu): for moduli [l0, l1), with residue
+// planes LR[l-l0][i][k] (Mp x Kp) and RR[l-l0][j][k] (Np x Kp), writes
+// res[l][j][i] = (sum_k LR*RR) mod m_l.  K range per output tile follows the
+// triangle (tri_left: rows of Lft; else columns of Rgt).
+struct OzGemmLaunch {
+  const uint16_t *LR, *RR;
+  uint8_t *res;
+  int64_t Mp, Np, Kp, M, N, K;
+  int l0, l1;
+  bool tri_left, tri_lower;
+  int *status;
+  int num_sms;
+};
+int launch_oz_gemm(const OzGemmLaunch &L, cudaStream_t st, const char **why);
+
+}  // namespace uvt

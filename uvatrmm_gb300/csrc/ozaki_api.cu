@@ -1,0 +1,196 @@
+// C ABI of the Ozaki-style emulated FP64 TRMM (see ozaki.cuh for the method).
+#include <algorithm>
+#include <cstring>
+#include <string>
+
+#include "api_internal.h"
+#include "common.cuh"
+#include "ozaki.cuh"
+
+namespace uvt {
+namespace {
+
+constexpr int kErrSamples = 8;
+
+// Builds the two residue operands of the canonical GEMM for a normalised TRMM.
+void operands(const Trmm &t, const double *dA, int64_t lda, const double *dB, int64_t ldb, OzOperand &L,
+              OzOperand &R) {
+  const bool lower = (t.uplo == CblasLower) != (t.trans != 0);
+  if (t.side == CblasLeft) {
+    // Lft = op(A) (m x m), Rgt = B (m x n).
+    L = OzOperand{dA, lda, t.m, t.m, t.trans != 0, true, true, lower, t.unit != 0};
+    R = OzOperand{dB, ldb, t.n, t.m, true, false, false, false, false};
+  } else {
+    // Lft = B (m x n), Rgt = op(A) (n x n): Rgt[k, j] = op(A)[k, j].
+    L = OzOperand{dB, ldb, t.m, t.n, false, false, false, false, false};
+    R = OzOperand{dA, lda, t.n, t.n, t.trans == 0, true, false, lower, t.unit != 0};
+  }
+}
+
+int ozaki_device(uvatrmm_handle_t h, int layout, int side, int uplo, int transa, int diag, int64_t m, int64_t n,
+                 double alpha, const double *dA, int64_t lda, double *dB, int64_t ldb, int moduli, double *relerr,
+                 int *bits_out) {
+  if (int bad = check_args(layout, side, uplo, transa, diag, m, n, lda, ldb))
+    return fail(UVATRMM_EINVAL, "parameter " + std::to_string(bad) + " had an illegal value");
+  if (moduli != 0 && (moduli < 2 || moduli > kMaxModuli))
+    return fail(UVATRMM_EINVAL, "moduli must be 0 (automatic) or 2.." + std::to_string(kMaxModuli));
+  const Trmm t = normalise(layout, side, uplo, transa, diag, m, n, alpha);
+  if (relerr) *relerr = 0.0;
+  if (t.m == 0 || t.n == 0) return ok();
+  if (alpha == 0.0) {
+    cudaError_t e = cudaMemset2DAsync(dB, ldb * 8, 0, t.m * 8, t.n, h->stream);
+    return e == cudaSuccess ? ok() : cuda_fail(e, "zero fill");
+  }
+  OzOperand L, R;
+  operands(t, dA, lda, dB, ldb, L, R);
+  OzPlan plan;
+  plan.M = t.m;
+  plan.N = t.n;
+  plan.K = t.side == CblasLeft ? t.m : t.n;
+  plan.n_moduli = moduli ? moduli : ozaki_auto_moduli(plan.K);
+  plan.bits = ozaki_bits(plan.n_moduli, plan.K);
+  plan.Mp = round_up(plan.M, 128);
+  plan.Np = round_up(plan.N, 256);
+  plan.Kp = round_up(plan.K, 64);
+  if (bits_out) *bits_out = plan.bits;
+
+  // Residue planes per modulus: (Mp + Np) x Kp bf16; passes of G moduli.
+  const int64_t per_mod = (plan.Mp + plan.Np) * plan.Kp * 2;
+  int G = (int)std::max<int64_t>(1, std::min<int64_t>(plan.n_moduli, (h->ozaki_scratch_mb << 20) / per_mod));
+  int *e = static_cast<int *>(workspace(h, 4, (size_t)(plan.Mp + plan.Np) * sizeof(int)));
+  uint8_t *res = static_cast<uint8_t *>(workspace(h, 6, (size_t)plan.n_moduli * plan.Mp * plan.Np));
+  uint16_t *planes = static_cast<uint16_t *>(workspace(h, 5, (size_t)G * per_mod));
+  if (!e || !res || !planes) return uvatrmm_last_status();
+  int *e_row = e, *e_col = e + plan.Mp;
+
+  // Error estimate: keep the sampled inputs (columns of B for side Left,
+  // rows for side Right) before B is overwritten.
+  const int S = relerr ? (int)std::min<int64_t>(kErrSamples, t.side == CblasLeft ? t.n : t.m) : 0;
+  double *samp = nullptr;
+  const int64_t len = t.side == CblasLeft ? t.m : t.n;  // entries per sampled column / row
+  if (S) {
+    samp = static_cast<double *>(workspace(h, 7, (size_t)3 * S * round_up(len, 16) * 8));
+    if (!samp) return uvatrmm_last_status();
+    const int64_t cnt = t.side == CblasLeft ? t.n : t.m;
+    for (int s = 0; s < S; ++s) {
+      const int64_t idx = S > 1 ? (cnt - 1) * s / (S - 1) : 0;
+      cudaError_t ce = t.side == CblasLeft
+                           ? cudaMemcpyAsync(samp + s * round_up(len, 16), dB + idx * ldb, len * 8,
+                                             cudaMemcpyDeviceToDevice, h->stream)
+                           : cudaMemcpy2DAsync(samp + s, S * 8, dB + idx, ldb * 8, 8, len,
+                                               cudaMemcpyDeviceToDevice, h->stream);
+      if (ce != cudaSuccess) return cuda_fail(ce, "error-estimate sample");
+    }
+  }
+
+  int rc = oz_scales(L, e_row, h->stream);
+  if (rc == UVATRMM_OK) rc = oz_scales(R, e_col, h->stream);
+  if (rc != UVATRMM_OK) return fail(rc, "Ozaki scaling failed to launch");
+  for (int l0 = 0; l0 < plan.n_moduli; l0 += G) {
+    const int l1 = std::min(plan.n_moduli, l0 + G);
+    uint16_t *LR = planes, *RR = planes + (int64_t)(l1 - l0) * plan.Mp * plan.Kp;
+    rc = oz_residues(L, e_row, plan.bits, l0, l1, plan.Mp, plan.Kp, LR, h->stream);
+    if (rc == UVATRMM_OK) rc = oz_residues(R, e_col, plan.bits, l0, l1, plan.Np, plan.Kp, RR, h->stream);
+    if (rc != UVATRMM_OK) return fail(rc, "Ozaki residue slicing failed to launch");
+    OzGemmLaunch g;
+    g.LR = LR;
+    g.RR = RR;
+    g.res = res;
+    g.Mp = plan.Mp; g.Np = plan.Np; g.Kp = plan.Kp;
+    g.M = plan.M; g.N = plan.N; g.K = plan.K;
+    g.l0 = l0; g.l1 = l1;
+    g.tri_left = t.side == CblasLeft;
+    g.tri_lower = (t.uplo == CblasLower) != (t.trans != 0);
+    g.status = h->dctl + 1;
+    g.num_sms = h->num_sms;
+    const char *why = nullptr;
+    rc = launch_oz_gemm(g, h->stream, &why);
+    if (rc != UVATRMM_OK) return fail(rc, why ? why : "residue GEMM launch failed");
+  }
+  rc = oz_reassemble(plan, res, e_row, e_col, t.alpha, dB, ldb, h->stream);
+  if (rc != UVATRMM_OK) return fail(rc, "CRT reassembly failed to launch");
+
+  if (S) {
+    // Plain FP64 reference for the sampled columns / rows, then the error.
+    const int64_t lp = round_up(len, 16);
+    double *ref = samp + (int64_t)S * lp, *got = samp + 2 * (int64_t)S * lp;
+    const int64_t cnt = t.side == CblasLeft ? t.n : t.m;
+    for (int s = 0; s < S; ++s) {
+      const int64_t idx = S > 1 ? (cnt - 1) * s / (S - 1) : 0;
+      cudaError_t ce = t.side == CblasLeft
+                           ? cudaMemcpyAsync(got + s * lp, dB + idx * ldb, len * 8, cudaMemcpyDeviceToDevice,
+                                             h->stream)
+                           : cudaMemcpy2DAsync(got + s, S * 8, dB + idx, ldb * 8, 8, len, cudaMemcpyDeviceToDevice,
+                                               h->stream);
+      if (ce != cudaSuccess) return cuda_fail(ce, "error-estimate sample");
+    }
+    if (t.side == CblasLeft)
+      rc = device_trmm(h, CblasColMajor, CblasLeft, t.uplo, t.trans ? CblasTrans : CblasNoTrans,
+                       t.unit ? CblasUnit : CblasNonUnit, t.m, S, t.alpha, dA, lda, samp, lp, ref, lp, false,
+                       h->schedule, h->shape);
+    else
+      rc = device_trmm(h, CblasColMajor, CblasRight, t.uplo, t.trans ? CblasTrans : CblasNoTrans,
+                       t.unit ? CblasUnit : CblasNonUnit, S, t.n, t.alpha, dA, lda, samp, S, ref, S, false,
+                       h->schedule, h->shape);
+    if (rc != UVATRMM_OK) return rc;
+    rc = t.side == CblasLeft ? rel_frobenius(h, len, S, got, lp, ref, lp, relerr)
+                             : rel_frobenius(h, S, len, got, S, ref, S, relerr);
+    if (rc != UVATRMM_OK) return rc;
+    rc = collect_status(h);
+    if (rc != UVATRMM_OK) return rc;
+  }
+  return ok();
+}
+
+}  // namespace
+}  // namespace uvt
+
+using namespace uvt;
+
+extern "C" {
+
+UVATRMM_API int uvatrmm_ozaki_plan(int64_t k, int moduli, int *moduli_out, int *bits_out) {
+  if (k < 0 || (moduli != 0 && (moduli < 2 || moduli > kMaxModuli))) return fail(UVATRMM_EINVAL, "invalid arguments");
+  const int n = moduli ? moduli : ozaki_auto_moduli(k);
+  if (moduli_out) *moduli_out = n;
+  if (bits_out) *bits_out = ozaki_bits(n, k);
+  return ok();
+}
+
+UVATRMM_API int uvatrmm_ozaki_dtrmm_device(uvatrmm_handle_t h, int layout, int side, int uplo, int transa, int diag,
+                                          int64_t m, int64_t n, double alpha, const double *dA, int64_t lda,
+                                          double *dB, int64_t ldb, int moduli, double *relerr_out, int *bits_out) {
+  if (!(h = resolve(h))) return uvatrmm_last_status();
+  std::lock_guard<std::mutex> g(h->mu);
+  return ozaki_device(h, layout, side, uplo, transa, diag, m, n, alpha, dA, lda, dB, ldb, moduli, relerr_out,
+                      bits_out);
+}
+
+UVATRMM_API int uvatrmm_ozaki_dtrmm(uvatrmm_handle_t h, int layout, int side, int uplo, int transa, int diag,
+                                   int64_t m, int64_t n, double alpha, const double *A, int64_t lda, double *B,
+                                   int64_t ldb, int moduli, double *relerr_out, int *bits_out) {
+  if (!(h = resolve(h))) return uvatrmm_last_status();
+  std::lock_guard<std::mutex> g(h->mu);
+  if (int bad = check_args(layout, side, uplo, transa, diag, m, n, lda, ldb))
+    return fail(UVATRMM_EINVAL, "parameter " + std::to_string(bad) + " had an illegal value");
+  const Trmm t = normalise(layout, side, uplo, transa, diag, m, n, alpha);
+  if (t.m == 0 || t.n == 0) return ok();
+  const int64_t ka = t.side == CblasLeft ? t.m : t.n;
+  const int64_t la = round_up(ka, 16), lb = round_up(t.m, 16);
+  double *dA = static_cast<double *>(workspace(h, 0, (size_t)la * ka * 8));
+  double *dB = static_cast<double *>(workspace(h, 2, (size_t)lb * t.n * 8));
+  if (!dA || !dB) return uvatrmm_last_status();
+  cudaError_t e = cudaMemcpy2DAsync(dA, la * 8, A, lda * 8, ka * 8, ka, cudaMemcpyHostToDevice, h->stream);
+  if (e == cudaSuccess) e = cudaMemcpy2DAsync(dB, lb * 8, B, ldb * 8, t.m * 8, t.n, cudaMemcpyHostToDevice, h->stream);
+  if (e != cudaSuccess) return cuda_fail(e, "host to device copy");
+  int rc = ozaki_device(h, CblasColMajor, t.side, t.uplo, t.trans ? CblasTrans : CblasNoTrans,
+                        t.unit ? CblasUnit : CblasNonUnit, t.m, t.n, t.alpha, dA, la, dB, lb, moduli, relerr_out,
+                        bits_out);
+  if (rc != UVATRMM_OK) return rc;
+  e = cudaMemcpy2DAsync(B, ldb * 8, dB, lb * 8, t.m * 8, t.n, cudaMemcpyDeviceToHost, h->stream);
+  if (e != cudaSuccess) return cuda_fail(e, "device to host copy");
+  rc = collect_status(h);
+  return rc == UVATRMM_OK ? ok() : rc;
+}
+
+}  // extern "C"

@@ -1,0 +1,401 @@
+// Exact residue GEMM on the 5th-generation tensor cores (tcgen05, sm_103a).
+//
+// For every modulus m_l and output tile (128 x 256): the K loop runs over
+// 64-wide bf16 slabs staged by TMA (128-byte swizzle, K-major) into a
+// 4-stage shared-memory ring; one thread issues tcgen05.mma.kind::f16
+// (bf16 x bf16 -> fp32 in TMEM, M=128 N=256 K=16).  Every 8 slabs (a K chunk
+// of 512) the accumulator is handed to the epilogue warps, which reduce it
+// modulo m_l in place (tcgen05.ld -> fp32 fold -> tcgen05.st) while the MMA
+// thread fills the other TMEM accumulator with the next chunk; the next chunk
+// for that accumulator then adds on top of the folded value.  Residues are
+// <= 128 in magnitude, so every value the accumulator ever holds is an
+// integer below 2^24 and fp32 accumulation is exact.  The last two chunks
+// are combined and the tile's residues (0 <= r < m_l) are written as bytes.
+//
+// Warp roles (192 threads, one CTA per SM): warp 0 TMA producer, warp 1 TMEM
+// owner + MMA issuer, warps 2-5 epilogue (each bound to its TMEM lane
+// quadrant, warp % 4).  All mbarrier waits are bounded; on expiry the kernel
+// records KERR_WAIT_TIMEOUT, drains its copies and MMAs, frees TMEM and exits.
+#include <algorithm>
+#include <cstring>
+
+#include "common.cuh"
+#include "ozaki.cuh"
+#include "tmap.cuh"
+
+namespace uvt {
+namespace {
+
+constexpr int BM = 128, BN = 256, BK = 64;
+constexpr int STAGES = 4;
+constexpr int CHUNK_SLABS = 8;  // K chunk of 512 between modular folds
+constexpr uint32_t A_BYTES = BM * BK * 2, B_BYTES = BN * BK * 2;
+constexpr uint32_t STAGE_BYTES = A_BYTES + B_BYTES;
+constexpr int NUM_THREADS = 192;
+constexpr uint32_t TMEM_COLS = 2 * BN;  // two fp32 accumulators of 256 columns
+constexpr size_t SMEM = 1024 + (size_t)STAGES * STAGE_BYTES + 256;
+// kind::f16 instruction descriptor: D fp32 (bits 4-5 = 1), A and B bf16
+// (bits 7-9 = 1, 10-12 = 1), both K-major, N/8 at bits 17-22, M/16 at 24-28.
+constexpr uint32_t IDESC = (1u << 4) | (1u << 7) | (1u << 10) | ((uint32_t)(BN >> 3) << 17) | ((uint32_t)(BM >> 4) << 24);
+
+struct GParams {
+  int64_t Mp, Np, M, N, K;
+  int l0, l1;
+  int tri_left, grows;   // triangle on Lft; work grows with the major index
+  int tri_lower;
+  int tiles_m, tiles_n, tiles_per_mod, total_tiles, group;
+  uint8_t *res;
+  int64_t plane;
+  int *status;
+  float mod_f[kMaxModuli];
+  float inv_f[kMaxModuli];
+};
+
+struct Tile {
+  int l, ti, tj, ks0, ks1;
+};
+
+__device__ __forceinline__ Tile decode(const GParams &p, int t) {
+  Tile T;
+  T.l = p.l0 + t / p.tiles_per_mod;
+  int r = t % p.tiles_per_mod;
+  const int n_maj = p.tri_left ? p.tiles_m : p.tiles_n, n_min = p.tri_left ? p.tiles_n : p.tiles_m;
+  // Raster: groups of `group` major tiles in longest-first order; inside a
+  // group the minor index is outer, so concurrent CTAs share both panels.
+  const int gspan = p.group * n_min;
+  const int g = r / gspan, within = r % gspan;
+  const int gsize = min(p.group, n_maj - g * p.group);
+  const int mi = within / gsize, rank = g * p.group + within % gsize;
+  const int ma = p.grows ? (n_maj - 1 - rank) : rank;
+  T.ti = p.tri_left ? ma : mi;
+  T.tj = p.tri_left ? mi : ma;
+  int64_t kb, ke;
+  if (p.tri_left) {
+    const int64_t i0 = (int64_t)T.ti * BM;
+    if (p.tri_lower) { kb = 0; ke = min(i0 + BM, p.K); }
+    else { kb = i0; ke = p.K; }
+  } else {
+    const int64_t j0 = (int64_t)T.tj * BN;
+    if (p.tri_lower) { kb = j0; ke = p.K; }
+    else { kb = 0; ke = min(j0 + BN, p.K); }
+  }
+  T.ks0 = (int)(kb / BK);
+  T.ks1 = (int)((ke + BK - 1) / BK);
+  return T;
+}
+
+// ---------------------------------------------------------------- tcgen05 wrappers
+__device__ __forceinline__ uint64_t sw128_desc(uint32_t saddr) {
+  uint64_t d = (uint64_t)((saddr & 0x3FFFFu) >> 4);
+  d |= (uint64_t)(16u >> 4) << 16;    // leading byte offset (unused for swizzled K-major)
+  d |= (uint64_t)(1024u >> 4) << 32;  // stride byte offset: 8 rows x 128 B
+  d |= (uint64_t)1 << 46;             // descriptor version
+  d |= (uint64_t)2 << 61;             // 128-byte swizzle
+  return d;
+}
+
+__device__ __forceinline__ void umma_bf16(uint32_t d_tmem, uint64_t a, uint64_t b, uint32_t acc) {
+  asm volatile(
+      "{\n .reg .pred p;\n setp.ne.b32 p, %4, 0;\n"
+      " tcgen05.mma.cta_group::1.kind::f16 [%0], %1, %2, %3, p;\n}\n" ::"r"(d_tmem),
+      "l"(a), "l"(b), "r"(IDESC), "r"(acc)
+      : "memory");
+}
+
+__device__ __forceinline__ void umma_commit(uint64_t *bar) {
+  asm volatile("tcgen05.commit.cta_group::1.mbarrier::arrive::one.shared::cluster.b64 [%0];" ::"r"(smem_u32(bar))
+               : "memory");
+}
+
+__device__ __forceinline__ void tc_fence_before() { asm volatile("tcgen05.fence::before_thread_sync;" ::: "memory"); }
+__device__ __forceinline__ void tc_fence_after() { asm volatile("tcgen05.fence::after_thread_sync;" ::: "memory"); }
+
+__device__ __forceinline__ void tmem_ld32(uint32_t taddr, uint32_t (&v)[32]) {
+  asm volatile(
+      "tcgen05.ld.sync.aligned.32x32b.x32.b32 {%0,%1,%2,%3,%4,%5,%6,%7,%8,%9,%10,%11,%12,%13,%14,%15,"
+      "%16,%17,%18,%19,%20,%21,%22,%23,%24,%25,%26,%27,%28,%29,%30,%31}, [%32];"
+      : "=r"(v[0]), "=r"(v[1]), "=r"(v[2]), "=r"(v[3]), "=r"(v[4]), "=r"(v[5]), "=r"(v[6]), "=r"(v[7]),
+        "=r"(v[8]), "=r"(v[9]), "=r"(v[10]), "=r"(v[11]), "=r"(v[12]), "=r"(v[13]), "=r"(v[14]), "=r"(v[15]),
+        "=r"(v[16]), "=r"(v[17]), "=r"(v[18]), "=r"(v[19]), "=r"(v[20]), "=r"(v[21]), "=r"(v[22]), "=r"(v[23]),
+        "=r"(v[24]), "=r"(v[25]), "=r"(v[26]), "=r"(v[27]), "=r"(v[28]), "=r"(v[29]), "=r"(v[30]), "=r"(v[31])
+      : "r"(taddr)
+      : "memory");
+}
+
+__device__ __forceinline__ void tmem_st32(uint32_t taddr, const uint32_t (&v)[32]) {
+  asm volatile(
+      "tcgen05.st.sync.aligned.32x32b.x32.b32 [%0], {%1,%2,%3,%4,%5,%6,%7,%8,%9,%10,%11,%12,%13,%14,%15,%16,"
+      "%17,%18,%19,%20,%21,%22,%23,%24,%25,%26,%27,%28,%29,%30,%31,%32};" ::"r"(taddr),
+      "r"(v[0]), "r"(v[1]), "r"(v[2]), "r"(v[3]), "r"(v[4]), "r"(v[5]), "r"(v[6]), "r"(v[7]), "r"(v[8]),
+      "r"(v[9]), "r"(v[10]), "r"(v[11]), "r"(v[12]), "r"(v[13]), "r"(v[14]), "r"(v[15]), "r"(v[16]), "r"(v[17]),
+      "r"(v[18]), "r"(v[19]), "r"(v[20]), "r"(v[21]), "r"(v[22]), "r"(v[23]), "r"(v[24]), "r"(v[25]), "r"(v[26]),
+      "r"(v[27]), "r"(v[28]), "r"(v[29]), "r"(v[30]), "r"(v[31])
+      : "memory");
+}
+
+__device__ __forceinline__ void tmem_wait_ld() { asm volatile("tcgen05.wait::ld.sync.aligned;" ::: "memory"); }
+__device__ __forceinline__ void tmem_wait_st() { asm volatile("tcgen05.wait::st.sync.aligned;" ::: "memory"); }
+
+// r = v mod m in [0, m) for an fp32 integer v (|v| < 2^25).
+__device__ __forceinline__ float mod_pos(float v, float m, float inv) {
+  float q = floorf(v * inv);
+  float r = fmaf(-q, m, v);
+  if (r < 0.f) r += m;
+  if (r >= m) r -= m;
+  return r;
+}
+
+// ---------------------------------------------------------------- kernel
+__global__ void __launch_bounds__(NUM_THREADS, 1)
+    oz_gemm_kernel(const __grid_constant__ CUtensorMap tmA, const __grid_constant__ CUtensorMap tmB,
+                   const __grid_constant__ GParams p) {
+  extern __shared__ uint8_t smem_raw[];
+  uint8_t *base = reinterpret_cast<uint8_t *>((reinterpret_cast<uintptr_t>(smem_raw) + 1023) & ~uintptr_t(1023));
+  uint64_t *bars = reinterpret_cast<uint64_t *>(base + STAGES * STAGE_BYTES);
+  uint64_t *full = bars, *empty = bars + STAGES;
+  uint64_t *cdone = bars + 2 * STAGES, *afree = cdone + 2, *drain = afree + 2;
+  uint32_t *tmem_slot = reinterpret_cast<uint32_t *>(drain + 1);
+  auto smA = [&](int s) { return base + s * STAGE_BYTES; };
+  auto smB = [&](int s) { return base + s * STAGE_BYTES + A_BYTES; };
+
+  const int warp = threadIdx.x >> 5, lane = threadIdx.x & 31;
+  if (threadIdx.x == 0) {
+    for (int s = 0; s < STAGES; ++s) {
+      mbar_init(&full[s], 1);
+      mbar_init(&empty[s], 1);
+    }
+    for (int b = 0; b < 2; ++b) {
+      mbar_init(&cdone[b], 1);
+      mbar_init(&afree[b], 4);
+    }
+    mbar_init(drain, 1);
+    fence_barrier_init();
+  }
+  if (warp == 1) {
+    asm volatile("tcgen05.alloc.cta_group::1.sync.aligned.shared::cta.b32 [%0], %1;" ::"r"(smem_u32(tmem_slot)),
+                 "r"(TMEM_COLS)
+                 : "memory");
+    asm volatile("tcgen05.relinquish_alloc_permit.cta_group::1.sync.aligned;" ::: "memory");
+    tc_fence_before();
+  }
+  __syncthreads();
+  tc_fence_after();
+  const uint32_t tmem_base = *reinterpret_cast<volatile uint32_t *>(tmem_slot);
+
+  if (warp == 0) {
+    // ------------------------------------------------------------ TMA producer
+    if (lane == 0) {
+      tma_prefetch_desc(&tmA);
+      tma_prefetch_desc(&tmB);
+      int s = 0;
+      uint32_t ph = 0, issued = 0, last_ph[STAGES] = {0, 0, 0, 0};
+      bool ok = true;
+      for (int t = blockIdx.x; ok && t < p.total_tiles; t += gridDim.x) {
+        const Tile T = decode(p, t);
+        const int ya = (int)((T.l - p.l0) * p.Mp + (int64_t)T.ti * BM);
+        const int yb = (int)((T.l - p.l0) * p.Np + (int64_t)T.tj * BN);
+        for (int ks = T.ks0; ks < T.ks1; ++ks) {
+          if (!mbar_wait_bounded(&empty[s], ph ^ 1)) {
+            record_error(p.status, KERR_WAIT_TIMEOUT);
+            ok = false;
+            break;
+          }
+          mbar_arrive_expect_tx(&full[s], STAGE_BYTES);
+          tma_load_2d(smA(s), &tmA, ks * BK, ya, &full[s]);
+          tma_load_2d(smB(s), &tmB, ks * BK, yb, &full[s]);
+          issued |= 1u << s;
+          last_ph[s] = ph;
+          if (++s == STAGES) { s = 0; ph ^= 1; }
+        }
+      }
+      for (int st = 0; st < STAGES; ++st)
+        if ((issued >> st) & 1u)
+          if (!mbar_wait_bounded(&full[st], last_ph[st])) record_error(p.status, KERR_WAIT_TIMEOUT);
+    }
+  } else if (warp == 1) {
+    // ------------------------------------------------------------ MMA issuer
+    if (lane == 0) {
+      int s = 0;
+      uint32_t ph = 0, uses[2] = {0, 0};
+      bool ok = true, any = false;
+      for (int t = blockIdx.x; ok && t < p.total_tiles; t += gridDim.x) {
+        const Tile T = decode(p, t);
+        const int nslab = T.ks1 - T.ks0;
+        const int nchunk = (nslab + CHUNK_SLABS - 1) / CHUNK_SLABS;
+        for (int c = 0; ok && c < nchunk; ++c) {
+          const int b = c & 1;
+          if (!mbar_wait_bounded(&afree[b], (uses[b] & 1u) ^ 1u)) {
+            record_error(p.status, KERR_WAIT_TIMEOUT);
+            ok = false;
+            break;
+          }
+          tc_fence_after();
+          const uint32_t d_tmem = tmem_base + (uint32_t)(b * BN);
+          const int sl0 = c * CHUNK_SLABS, sl1 = min(nslab, sl0 + CHUNK_SLABS);
+          for (int sl = sl0; sl < sl1; ++sl) {
+            if (!mbar_wait_bounded(&full[s], ph)) {
+              record_error(p.status, KERR_WAIT_TIMEOUT);
+              ok = false;
+              break;
+            }
+            tc_fence_after();
+            const uint32_t a0 = smem_u32(smA(s)), b0 = smem_u32(smB(s));
+#pragma unroll
+            for (int kk = 0; kk < BK / 16; ++kk) {
+              const uint32_t acc = (c >= 2 || sl > sl0 || kk > 0) ? 1u : 0u;
+              umma_bf16(d_tmem, sw128_desc(a0 + kk * 32), sw128_desc(b0 + kk * 32), acc);
+            }
+            umma_commit(&empty[s]);
+            any = true;
+            if (++s == STAGES) { s = 0; ph ^= 1; }
+          }
+          if (!ok) break;
+          umma_commit(&cdone[b]);
+          ++uses[b];
+        }
+      }
+      // Drain: all MMAs this thread issued complete before TMEM is freed.
+      if (any) {
+        umma_commit(drain);
+        if (!mbar_wait_bounded(drain, 0)) record_error(p.status, KERR_WAIT_TIMEOUT);
+      }
+    }
+  } else {
+    // ------------------------------------------------------------ epilogue
+    const int quad = warp & 3;
+    const int row = quad * 32 + lane;
+    const uint32_t lane_base = tmem_base + ((uint32_t)(quad * 32) << 16);
+    uint32_t uses[2] = {0, 0};
+    bool ok = true;
+    for (int t = blockIdx.x; ok && t < p.total_tiles; t += gridDim.x) {
+      const Tile T = decode(p, t);
+      const int nslab = T.ks1 - T.ks0;
+      const int nchunk = (nslab + CHUNK_SLABS - 1) / CHUNK_SLABS;
+      const float m = p.mod_f[T.l], inv = p.inv_f[T.l];
+      for (int c = 0; c < nchunk; ++c) {
+        const int b = c & 1;
+        if (!mbar_wait_bounded(&cdone[b], uses[b] & 1u)) {
+          record_error(p.status, KERR_WAIT_TIMEOUT);
+          ok = false;
+          break;
+        }
+        ++uses[b];
+        tc_fence_after();
+        if (c < nchunk - 2) {
+          // Fold: acc := acc - m * rint(acc / m), exact in fp32.
+#pragma unroll 1
+          for (int cb = 0; cb < BN / 32; ++cb) {
+            uint32_t v[32];
+            const uint32_t ta = lane_base + (uint32_t)(b * BN + cb * 32);
+            tmem_ld32(ta, v);
+            tmem_wait_ld();
+#pragma unroll
+            for (int e = 0; e < 32; ++e) {
+              const float x = __uint_as_float(v[e]);
+              v[e] = __float_as_uint(fmaf(-rintf(x * inv), m, x));
+            }
+            tmem_st32(ta, v);
+          }
+          tmem_wait_st();
+          tc_fence_before();
+          __syncwarp();
+          if (lane == 0) mbar_arrive(&afree[b]);
+        } else if (c == nchunk - 1) {
+          // Final: residue of (acc[b] + acc[other]) as bytes.
+          const bool two = nchunk >= 2;
+          const int64_t i = (int64_t)T.ti * BM + row;
+          uint8_t *out = p.res + (int64_t)T.l * p.plane + i;
+#pragma unroll 1
+          for (int cb = 0; cb < BN / 32; ++cb) {
+            uint32_t v[32], w[32];
+            tmem_ld32(lane_base + (uint32_t)(b * BN + cb * 32), v);
+            if (two) tmem_ld32(lane_base + (uint32_t)((b ^ 1) * BN + cb * 32), w);
+            tmem_wait_ld();
+            const int64_t j0 = (int64_t)T.tj * BN + cb * 32;
+#pragma unroll
+            for (int e = 0; e < 32; ++e) {
+              float r = mod_pos(__uint_as_float(v[e]), m, inv);
+              if (two) {
+                r += mod_pos(__uint_as_float(w[e]), m, inv);
+                if (r >= m) r -= m;
+              }
+              out[(j0 + e) * p.Mp] = (uint8_t)(int)r;
+            }
+          }
+          tc_fence_before();
+          __syncwarp();
+          if (lane == 0) {
+            mbar_arrive(&afree[b]);
+            if (two) mbar_arrive(&afree[b ^ 1]);
+          }
+        }
+        // c == nchunk - 2: kept for the final combine, released there.
+      }
+    }
+  }
+  __syncthreads();
+  if (warp == 1) {
+    tc_fence_after();
+    asm volatile("tcgen05.dealloc.cta_group::1.sync.aligned.b32 %0, %1;" ::"r"(tmem_base), "r"(TMEM_COLS)
+                 : "memory");
+  }
+}
+
+}  // namespace
+
+int launch_oz_gemm(const OzGemmLaunch &L, cudaStream_t st, const char **why) {
+  *why = nullptr;
+  if (L.l1 <= L.l0 || L.M <= 0 || L.N <= 0 || L.K <= 0) return UVATRMM_OK;
+  if (L.Mp % BM || L.Np % BN || L.Kp % BK) {
+    *why = "residue planes are not padded to the tile sizes";
+    return UVATRMM_EINVAL;
+  }
+  const int nmod = L.l1 - L.l0;
+  if ((int64_t)nmod * L.Mp > INT32_MAX || (int64_t)nmod * L.Np > INT32_MAX || L.Kp > INT32_MAX) {
+    *why = "problem too large for one residue pass";
+    return UVATRMM_EINVAL;
+  }
+  CUtensorMap tmA, tmB;
+  if (make_tmap_2d(&tmA, CU_TENSOR_MAP_DATA_TYPE_BFLOAT16, 2, L.LR, L.Kp, nmod * L.Mp, L.Kp * 2, BK, BM, true) ||
+      make_tmap_2d(&tmB, CU_TENSOR_MAP_DATA_TYPE_BFLOAT16, 2, L.RR, L.Kp, nmod * L.Np, L.Kp * 2, BK, BN, true)) {
+    *why = "tensor map encoding failed for the residue planes";
+    return UVATRMM_EDEVICE;
+  }
+  GParams g;
+  memset(&g, 0, sizeof(g));
+  g.Mp = L.Mp; g.Np = L.Np; g.M = L.M; g.N = L.N; g.K = L.K;
+  g.l0 = L.l0; g.l1 = L.l1;
+  g.tri_left = L.tri_left;
+  g.tri_lower = L.tri_lower;
+  g.grows = L.tri_left ? L.tri_lower : !L.tri_lower;
+  g.tiles_m = (int)(L.Mp / BM);
+  g.tiles_n = (int)(L.Np / BN);
+  g.tiles_per_mod = g.tiles_m * g.tiles_n;
+  g.total_tiles = g.tiles_per_mod * nmod;
+  g.group = 8;
+  g.res = L.res;
+  g.plane = L.Mp * L.Np;
+  g.status = L.status;
+  for (int l = 0; l < kMaxModuli; ++l) {
+    g.mod_f[l] = (float)kModuli[l];
+    g.inv_f[l] = 1.0f / (float)kModuli[l];
+  }
+  static bool attr = false;
+  if (!attr) {
+    if (cudaFuncSetAttribute(oz_gemm_kernel, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)SMEM) != cudaSuccess) {
+      *why = "cannot reserve shared memory for the residue GEMM";
+      return UVATRMM_EDEVICE;
+    }
+    attr = true;
+  }
+  const int grid = std::min(L.num_sms, g.total_tiles);
+  oz_gemm_kernel<<<grid, NUM_THREADS, SMEM, st>>>(tmA, tmB, g);
+  cudaError_t e = cudaGetLastError();
+  if (e != cudaSuccess) {
+    *why = cudaGetErrorString(e);
+    return UVATRMM_EDEVICE;
+  }
+  return UVATRMM_OK;
+}
+
+}  // namespace uvt
