@@ -247,7 +247,117 @@ def run_gpu(args, ws, rank, local):
         "clocks": clocks,
         "check": {"sampled_rel_fro_err_vs_openblas": relerr},
     }
+    del hA, hB, hB0
+    if not args.no_ozaki:
+        out["ozaki"] = run_ozaki(args, h, dev, stream, rank, achieved)
     return out
+
+
+def bf16_peak():
+    """Sustained cuBLAS bf16 TFLOP/s from MEASURED_PEAKS.json (driver-measured), else the fallback."""
+    try:
+        with open(os.path.join(ROOT, "MEASURED_PEAKS.json")) as f:
+            return float(json.load(f)["bf16_tflops_sustained"]), "measured (MEASURED_PEAKS.json, sustained)"
+    except Exception:
+        return 1700.0, "fallback (profiling recipe, sustained)"
+
+
+def ozaki_mma_flops(m, n, moduli, side_left=True, lower=True):
+    """bf16 MMA flops the residue GEMM issues for one call (tile-exact)."""
+    BM, BN, BK = 128, 256, 64
+    Mp, Np = -(-m // BM) * BM, -(-n // BN) * BN
+    K = m if side_left else n
+    total = 0
+    if side_left:
+        for ti in range(Mp // BM):
+            i0 = ti * BM
+            kb, ke = (0, min(i0 + BM, K)) if lower else (i0, K)
+            total += (Np // BN) * ((ke + BK - 1) // BK - kb // BK) * BK
+    else:
+        for tj in range(Np // BN):
+            j0 = tj * BN
+            kb, ke = (j0, K) if lower else (0, min(j0 + BN, K))
+            total += (Mp // BM) * ((ke + BK - 1) // BK - kb // BK) * BK
+    return 2.0 * BM * BN * total * moduli
+
+
+def run_ozaki(args, h, dev, stream, rank, plain_tflops):
+    """Ozaki emulated FP64 TRMM at the precision configuration: m = n = 32768,
+    side=L, uplo=U, trans=T, entries uniform[-1,1) * 2^k, k uniform in
+    [-20, 20], seed 2; automatic slice count timed, slice counts swept for
+    the error against the double-double oracle on sampled columns."""
+    import numpy as np
+    import torch
+
+    import uvatrmm_gb300 as u
+    m = n = args.ozaki_n
+    C_, Le, Up, Tr, NU = u.COL, u.LEFT, u.UPPER, u.TRANS, u.NONUNIT
+    dA = torch.empty(m * m, dtype=torch.float64, device=dev)
+    dB0 = torch.empty(m * n, dtype=torch.float64, device=dev)
+    dB = torch.empty(m * n, dtype=torch.float64, device=dev)
+    h.gen_uniform(2, 0, m, m, dA, 1, m, tri="U", spread=20)
+    h.gen_uniform(2, 1, m, n, dB0, 1, m, spread=20)
+    h.sync()
+    h.set_option("stage_timing", 1)
+    moduli, bits = u.ozaki_plan(m)
+
+    def step(mo=0, want_err=False):
+        dB.copy_(dB0)
+        ev0, ev1 = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
+        ev0.record(stream)
+        err, b = h.ozaki_device(C_, Le, Up, Tr, NU, m, n, 1.0, dA, m, dB, m, moduli=mo, want_err=want_err)
+        ev1.record(stream)
+        h.sync()
+        return ev0.elapsed_time(ev1), err, b
+
+    for _ in range(max(1, args.warmup - 2)):
+        step()
+    times, stages = [], []
+    for _ in range(args.ozaki_steps):
+        ms, _, _ = step()
+        times.append(ms)
+        stages.append(h.stage_times())
+    t_ms = statistics.mean(times)
+    tflops = float(m) * m * n / (t_ms * 1e-3) / 1e12
+    st = [statistics.mean(s[k] for s in stages) for k in range(4)]
+    gemm_flops = ozaki_mma_flops(m, n, moduli, True, True)
+    peak, peak_src = bf16_peak()
+    gemm_tflops = gemm_flops / (st[2] * 1e-3) / 1e12
+
+    sweep = []
+    if rank == 0 and args.check:
+        from oracle import oracle as orc
+        sel = [1, n // 3, (2 * n) // 3, n - 2]
+        A = dA.cpu().numpy()
+        B = dB0.cpu().numpy()
+        Bs = np.concatenate([B[j * m:(j + 1) * m] for j in sel])
+        orc.lib()
+        ref = orc.dtrmm_dd(C_, Le, Up, Tr, NU, m, len(sel), 1.0, A, m, Bs, m)
+        del A
+        for mo in sorted({14, 15, 16, 17, 18, 19, 20, moduli}):
+            _, est, b = step(mo, want_err=True)
+            got = np.stack([dB[j * m:(j + 1) * m].cpu().numpy() for j in sel], axis=1)
+            sweep.append({"moduli": mo, "bits": b, "rel_fro_err_vs_dd_oracle": float(
+                np.linalg.norm(got - ref) / np.linalg.norm(ref)), "rel_fro_err_vs_plain_fp64_gpu": est})
+    h.set_option("stage_timing", 0)
+    del dA, dB0, dB
+    torch.cuda.empty_cache()
+    auto = next((s for s in sweep if s["moduli"] == moduli), None)
+    return {
+        "workload": f"Ozaki emulated FP64 TRMM m=n={m}, side=L uplo=U trans=T diag=N alpha=1, "
+                    "entries uniform[-1,1)*2^k, k in [-20,20], seed 2",
+        "value": round(tflops, 3), "unit": "TFLOP/s (m^2 n FP64-equivalent flops)", "steps": len(times),
+        "ms_per_step": round(t_ms, 3), "moduli": moduli, "bits": bits,
+        "rel_fro_err_vs_dd_oracle": auto["rel_fro_err_vs_dd_oracle"] if auto else None,
+        "speedup_vs_plain_fp64": round(tflops / plain_tflops, 2),
+        "stage_ms": {"scaling": round(st[0], 3), "slicing": round(st[1], 3), "residue_gemm": round(st[2], 3),
+                     "reassembly": round(st[3], 3)},
+        "roofline": {"bound": "tensor", "kernel": "oz_gemm_kernel (tcgen05 kind::f16, bf16 -> fp32)",
+                     "achieved": round(gemm_tflops, 2), "peak": peak, "unit": "TFLOP/s",
+                     "frac": round(gemm_tflops / peak, 4), "peak_source": peak_src,
+                     "flops": "bf16 MMA flops issued (tile-exact) / residue-GEMM GPU time"},
+        "slice_sweep": sweep,
+    }
 
 
 def main():
@@ -261,6 +371,9 @@ def main():
     ap.add_argument("--cpu-n", type=int, default=16384)
     ap.add_argument("--no-cpu-baseline", action="store_true")
     ap.add_argument("--no-check", dest="check", action="store_false")
+    ap.add_argument("--no-ozaki", action="store_true")
+    ap.add_argument("--ozaki-n", type=int, default=32768)
+    ap.add_argument("--ozaki-steps", type=int, default=3)
     args = ap.parse_args()
     ws, rank, local = dist_env()
     threads = os.cpu_count() or 1

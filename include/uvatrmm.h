@@ -89,7 +89,8 @@ typedef enum {
   UVATRMM_OPT_SCHEDULE = 2, /* UVATRMM_SCHED_*    tile-to-SM assignment */
   UVATRMM_OPT_SHAPE = 3,    /* UVATRMM_SHAPE_*    diagonal tile geometry */
   UVATRMM_OPT_TILE = 4,     /* 0 = automatic, 64 or 128: output tile edge */
-  UVATRMM_OPT_OZAKI_SCRATCH_MB = 5 /* Ozaki residue-plane budget per pass, MiB (default 49152) */
+  UVATRMM_OPT_OZAKI_SCRATCH_MB = 5, /* Ozaki residue-plane budget per pass, MiB (default 49152) */
+  UVATRMM_OPT_STAGE_TIMING = 6      /* 1: time the stages of each Ozaki call (uvatrmm_stage_times) */
 } uvatrmm_option;
 typedef enum { UVATRMM_ENGINE_DFMA = 0, UVATRMM_ENGINE_DMMA = 1 } uvatrmm_engine;
 /* DYNAMIC: persistent CTAs pull tiles in longest-first order.
@@ -138,6 +139,10 @@ UVATRMM_API int uvatrmm_ozaki_dtrmm_device(uvatrmm_handle_t handle, int layout, 
 UVATRMM_API int uvatrmm_ozaki_dtrmm(uvatrmm_handle_t handle, int layout, int side, int uplo, int transa, int diag,
                                    int64_t m, int64_t n, double alpha, const double *A, int64_t lda, double *B,
                                    int64_t ldb, int moduli, double *relerr_out, int *bits_out);
+/* GPU milliseconds of the last Ozaki call's stages: [0] scaling, [1] residue
+ * slicing, [2] residue GEMMs, [3] CRT reassembly (needs
+ * UVATRMM_OPT_STAGE_TIMING = 1; synchronises). */
+UVATRMM_API int uvatrmm_stage_times(uvatrmm_handle_t handle, double *ms4);
 /* Residue slices the automatic choice uses for inner dimension k, and the
  * bits per scaled entry that `moduli` slices give for it. */
 UVATRMM_API int uvatrmm_ozaki_plan(int64_t k, int moduli, int *moduli_out, int *bits_out);

@@ -125,7 +125,7 @@ def test_ozaki_zero_rows_and_alpha_zero(handle):
     m, n = 50, 40
     A, lda, B, ldb = make_problem(COL, LEFT, LOWER, m, n)
     B2 = B.copy()
-    B2[5 * ldb:6 * ldb - 2] = 0.0  # one zero column of B
+    B2[5 * ldb:5 * ldb + m] = 0.0  # one zero column of B
     ref = dd_reference(COL, LEFT, LOWER, NOTRANS, NONUNIT, m, n, 1.0, A, lda, B2, ldb)
     got = B2.copy()
     handle.ozaki(COL, LEFT, LOWER, NOTRANS, NONUNIT, m, n, 1.0, A, lda, got, ldb)

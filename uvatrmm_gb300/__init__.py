@@ -61,8 +61,15 @@ class Handle:
         check(lib().uvatrmm_set_stream(self.h, C.c_void_p(int(s) if s else 0)))
 
     def set_option(self, name: str, value: int) -> None:
-        key = {"engine": OPT_ENGINE, "schedule": OPT_SCHEDULE, "shape": OPT_SHAPE, "tile": OPT_TILE}[name]
+        key = {"engine": OPT_ENGINE, "schedule": OPT_SCHEDULE, "shape": OPT_SHAPE, "tile": OPT_TILE,
+               "ozaki_scratch_mb": 5, "stage_timing": 6}[name]
         check(lib().uvatrmm_set_option(self.h, key, int(value)))
+
+    def stage_times(self):
+        """(scaling, slicing, GEMMs, reassembly) GPU ms of the last Ozaki call."""
+        buf = (C.c_double * 4)()
+        check(lib().uvatrmm_stage_times(self.h, buf))
+        return tuple(buf)
 
     # -- TRMM ------------------------------------------------------------
     def dtrmm(self, layout, side, uplo, transa, diag, m, n, alpha, A, lda, B, ldb) -> None:

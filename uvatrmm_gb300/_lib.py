@@ -33,6 +33,7 @@ SIGNATURES = {
     "uvatrmm_ozaki_dtrmm": (i32, [vp, i32, i32, i32, i32, i32, i64, i64, dbl, vp, i64, vp, i64, i32,
                                   C.POINTER(dbl), C.POINTER(i32)]),
     "uvatrmm_ozaki_plan": (i32, [i64, i32, C.POINTER(i32), C.POINTER(i32)]),
+    "uvatrmm_stage_times": (i32, [vp, C.POINTER(dbl)]),
     "uvatrmm_map_rows": (i32, [i32, u64, u32, u32, C.POINTER(u64), C.POINTER(u64)]),
     "uvatrmm_product": (i32, [vp, i64, i32, i32, vp, vp, vp, C.POINTER(dbl)]),
     "uvatrmm_gen_consecutive": (i32, [vp, i64, i32, vp]),

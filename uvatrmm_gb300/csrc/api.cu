@@ -256,6 +256,8 @@ UVATRMM_API int uvatrmm_destroy(uvatrmm_handle_t h) {
   if (h->dctl) cudaFree(h->dctl);
   if (h->ev0) cudaEventDestroy(h->ev0);
   if (h->ev1) cudaEventDestroy(h->ev1);
+  for (auto &ev : h->sev)
+    if (ev) cudaEventDestroy(ev);
   for (auto &d : tl_default)
     if (d == h) d = nullptr;
   delete h;
@@ -290,6 +292,13 @@ UVATRMM_API int uvatrmm_set_option(uvatrmm_handle_t h, int option, int value) {
     case UVATRMM_OPT_OZAKI_SCRATCH_MB:
       if (value < 64) break;
       h->ozaki_scratch_mb = value;
+      return ok();
+    case UVATRMM_OPT_STAGE_TIMING:
+      if (value != 0 && value != 1) break;
+      if (value && !h->sev[0])
+        for (auto &ev : h->sev)
+          if (cudaEventCreate(&ev) != cudaSuccess) return cuda_fail(cudaGetLastError(), "stage events");
+      h->stage_timing = value != 0;
       return ok();
     default:
       return fail(UVATRMM_EINVAL, "unknown option");

@@ -26,6 +26,13 @@ struct uvatrmm_handle_st {
   size_t ws_cap[kSlots] = {};
   int *dctl = nullptr;  // [0] tile counter, [1] kernel status word
   cudaEvent_t ev0 = nullptr, ev1 = nullptr;
+  // Per-stage GPU timing of the last Ozaki call (UVATRMM_OPT_STAGE_TIMING):
+  // events bracket scaling, each pass's slicing and GEMM, and reassembly.
+  bool stage_timing = false;
+  static constexpr int kStageEvents = 48;
+  cudaEvent_t sev[kStageEvents] = {};
+  int n_sev = 0;
+  int sev_kind[kStageEvents] = {};  // stage the interval ending at this event belongs to
   std::mutex mu;
 };
 

@@ -83,15 +83,25 @@ int ozaki_device(uvatrmm_handle_t h, int layout, int side, int uplo, int transa,
     }
   }
 
+  h->n_sev = 0;
+  auto mark = [&](int kind) {
+    if (h->stage_timing && h->n_sev < uvatrmm_handle_st::kStageEvents) {
+      h->sev_kind[h->n_sev] = kind;
+      cudaEventRecord(h->sev[h->n_sev++], h->stream);
+    }
+  };
+  mark(-1);
   int rc = oz_scales(L, e_row, h->stream);
   if (rc == UVATRMM_OK) rc = oz_scales(R, e_col, h->stream);
   if (rc != UVATRMM_OK) return fail(rc, "Ozaki scaling failed to launch");
+  mark(0);
   for (int l0 = 0; l0 < plan.n_moduli; l0 += G) {
     const int l1 = std::min(plan.n_moduli, l0 + G);
     uint16_t *LR = planes, *RR = planes + (int64_t)(l1 - l0) * plan.Mp * plan.Kp;
     rc = oz_residues(L, e_row, plan.bits, l0, l1, plan.Mp, plan.Kp, LR, h->stream);
     if (rc == UVATRMM_OK) rc = oz_residues(R, e_col, plan.bits, l0, l1, plan.Np, plan.Kp, RR, h->stream);
     if (rc != UVATRMM_OK) return fail(rc, "Ozaki residue slicing failed to launch");
+    mark(1);
     OzGemmLaunch g;
     g.LR = LR;
     g.RR = RR;
@@ -106,9 +116,11 @@ int ozaki_device(uvatrmm_handle_t h, int layout, int side, int uplo, int transa,
     const char *why = nullptr;
     rc = launch_oz_gemm(g, h->stream, &why);
     if (rc != UVATRMM_OK) return fail(rc, why ? why : "residue GEMM launch failed");
+    mark(2);
   }
   rc = oz_reassemble(plan, res, e_row, e_col, t.alpha, dB, ldb, h->stream);
   if (rc != UVATRMM_OK) return fail(rc, "CRT reassembly failed to launch");
+  mark(3);
 
   if (S) {
     // Plain FP64 reference for the sampled columns / rows, then the error.
@@ -148,6 +160,22 @@ int ozaki_device(uvatrmm_handle_t h, int layout, int side, int uplo, int transa,
 using namespace uvt;
 
 extern "C" {
+
+UVATRMM_API int uvatrmm_stage_times(uvatrmm_handle_t h, double *ms4) {
+  if (!(h = resolve(h))) return uvatrmm_last_status();
+  if (!ms4) return fail(UVATRMM_EINVAL, "ms4 is NULL");
+  std::lock_guard<std::mutex> g(h->mu);
+  for (int k = 0; k < 4; ++k) ms4[k] = 0.0;
+  if (h->n_sev < 2) return fail(UVATRMM_EINVAL, "no timed Ozaki call (enable UVATRMM_OPT_STAGE_TIMING)");
+  cudaError_t e = cudaEventSynchronize(h->sev[h->n_sev - 1]);
+  if (e != cudaSuccess) return cuda_fail(e, "stage timing");
+  for (int i = 1; i < h->n_sev; ++i) {
+    float ms = 0.f;
+    cudaEventElapsedTime(&ms, h->sev[i - 1], h->sev[i]);
+    if (h->sev_kind[i] >= 0 && h->sev_kind[i] < 4) ms4[h->sev_kind[i]] += ms;
+  }
+  return ok();
+}
 
 UVATRMM_API int uvatrmm_ozaki_plan(int64_t k, int moduli, int *moduli_out, int *bits_out) {
   if (k < 0 || (moduli != 0 && (moduli < 2 || moduli > kMaxModuli))) return fail(UVATRMM_EINVAL, "invalid arguments");
