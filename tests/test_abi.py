@@ -88,6 +88,6 @@ def test_ozaki_plan_is_monotonic(built):
         assert n == mo and bits >= prev
         prev = bits
     auto, bits = u.ozaki_plan(32768)
-    assert bits >= 56 and 14 <= auto <= 20
+    assert bits >= 52 and 14 <= auto <= 20
     with pytest.raises(u.UvatrmmError):
         u.ozaki_plan(100, 1)

@@ -39,7 +39,7 @@ def test_ozaki_all_variants_vs_double_double(handle, layout, side, uplo, trans, 
     pad = B == -7.0
     assert np.array_equal(got[pad], B[pad])
     assert rel_fro(got[~pad], ref[~pad]) <= TOL
-    assert bits >= 56 and err <= TOL
+    assert bits >= 52 and err <= TOL
 
 
 @pytest.mark.parametrize("K", [513, 1100, 2500])

@@ -34,7 +34,7 @@ constexpr int kModuli[kMaxModuli] = {256, 255, 253, 251, 247, 241, 239, 233, 229
 // Bits t kept per scaled operand entry for n moduli and inner dimension K:
 // the largest t with K * 2^(2t) < M / 4.
 int ozaki_bits(int n_moduli, int64_t K);
-// Slice count the automatic choice uses for inner dimension K (t >= 56).
+// Slice count the automatic choice uses for inner dimension K (t >= 52).
 int ozaki_auto_moduli(int64_t K);
 
 // One operand of the emulated product as the residue kernels see it:
