@@ -122,6 +122,27 @@ UVATRMM_API int uvatrmm_dtrmm_device_oop(uvatrmm_handle_t handle, int layout, in
                                          int diag, int64_t m, int64_t n, double alpha, const double *dA,
                                          int64_t lda, const double *dB, int64_t ldb, double *dC, int64_t ldc);
 
+/* The in-place device TRMM of uvatrmm_dtrmm_device for callers that cannot
+ * allocate device memory, e.g. a process whose device memory is all handed
+ * to its own pool or arena allocator, or a latency-bound loop that must not
+ * take the device-wide synchronisation of cudaMalloc/cudaFree.  No
+ * counterpart in the reference (which runs MKL on host memory).
+ *
+ * No handle: the call allocates nothing.  Its scratch (the staged copy of B,
+ * A when dA is not 16-byte aligned with an even lda, and two control words)
+ * lives in one fixed 64 MiB device array, so it rejects, with
+ * UVATRMM_EINVAL and a message, problems whose staged B (round_up(rows, 16)
+ * x cols doubles of the column-major view) plus any staged A exceed it.
+ * A device holds the array from the first call there until the process
+ * exits; that first call also looks up the array's device address and
+ * should come before any stream capture.  All calls on a device share the
+ * array: calls whose work overlaps on the GPU race.  Ordered on `stream` (a
+ * cudaStream_t, NULL = legacy default stream); returns after the result is
+ * in dB, with the kernel's status.  Plain DFMA engine, dynamic schedule. */
+UVATRMM_API int uvatrmm_dtrmm_device_noalloc(int layout, int side, int uplo, int transa, int diag, int64_t m,
+                                            int64_t n, double alpha, const double *dA, int64_t lda, double *dB,
+                                            int64_t ldb, void *stream);
+
 /* ---------------------------------------------------------------- Ozaki (emulated FP64) */
 /* The same TRMM computed exactly in integer arithmetic on the bf16 tensor
  * cores and rounded once to FP64 (Ozaki-style splitting with `moduli`

@@ -28,6 +28,7 @@ SIGNATURES = {
     "uvatrmm_dtrmm_device": (i32, [vp, i32, i32, i32, i32, i32, i64, i64, dbl, vp, i64, vp, i64]),
     "uvatrmm_dtrmm_device_oop": (i32, [vp, i32, i32, i32, i32, i32, i64, i64, dbl, vp, i64, vp, i64, vp, i64]),
     "uvatrmm_sync": (i32, [vp]),
+    "uvatrmm_dtrmm_device_noalloc": (i32, [i32, i32, i32, i32, i32, i64, i64, dbl, vp, i64, vp, i64, vp]),
     "uvatrmm_ozaki_dtrmm_device": (i32, [vp, i32, i32, i32, i32, i32, i64, i64, dbl, vp, i64, vp, i64, i32,
                                          C.POINTER(dbl), C.POINTER(i32)]),
     "uvatrmm_ozaki_dtrmm": (i32, [vp, i32, i32, i32, i32, i32, i64, i64, dbl, vp, i64, vp, i64, i32,
