@@ -90,7 +90,8 @@ typedef enum {
   UVATRMM_OPT_SHAPE = 3,    /* UVATRMM_SHAPE_*    diagonal tile geometry */
   UVATRMM_OPT_TILE = 4,     /* 0 = automatic, 64 or 128: output tile edge */
   UVATRMM_OPT_OZAKI_SCRATCH_MB = 5, /* Ozaki residue-plane budget per pass, MiB (default 49152) */
-  UVATRMM_OPT_STAGE_TIMING = 6      /* 1: time the stages of each Ozaki call (uvatrmm_stage_times) */
+  UVATRMM_OPT_STAGE_TIMING = 6,     /* 1: time the stages of each Ozaki call (uvatrmm_stage_times) */
+  UVATRMM_OPT_AUTOTUNE = 7          /* 1 (default): measure untuned shape buckets; 0: defaults only */
 } uvatrmm_option;
 typedef enum { UVATRMM_ENGINE_DFMA = 0, UVATRMM_ENGINE_DMMA = 1 } uvatrmm_engine;
 /* DYNAMIC: persistent CTAs pull tiles in longest-first order.
@@ -167,6 +168,51 @@ UVATRMM_API int uvatrmm_stage_times(uvatrmm_handle_t handle, double *ms4);
 /* Residue slices the automatic choice uses for inner dimension k, and the
  * bits per scaled entry that `moduli` slices give for it. */
 UVATRMM_API int uvatrmm_ozaki_plan(int64_t k, int moduli, int *moduli_out, int *bits_out);
+
+/* ---------------------------------------------------------------- grouped batches */
+/* No counterpart in the reference (one TRMM per process there).  Many TRMMs
+ * of any shape, side, uplo, trans and accuracy tier run as grouped
+ * persistent launches (one for every FP64 tile shape in use, one residue
+ * GEMM per Ozaki wave) captured once into a CUDA graph. */
+typedef enum { UVATRMM_TIER_FP64 = 0, UVATRMM_TIER_OZAKI = 1 } uvatrmm_tier;
+typedef struct {
+  int layout, side, uplo, transa, diag; /* CBLAS values */
+  int64_t m, n;
+  double alpha;
+  const double *A; /* device */
+  int64_t lda;
+  double *B; /* device, overwritten with the result */
+  int64_t ldb;
+  int tier;   /* uvatrmm_tier */
+  int moduli; /* Ozaki slices, 0 = automatic */
+} uvatrmm_trmm_problem;
+
+typedef struct uvatrmm_group_st *uvatrmm_group_t;
+/* Plans the batch: checks every problem, picks its tile shape (autotuner),
+ * sizes one workspace arena (Ozaki problems are processed in waves that fit
+ * UVATRMM_OPT_OZAKI_SCRATCH_MB), uploads the descriptors and captures the
+ * whole batch into a CUDA graph on the handle's stream.  The problems'
+ * buffers must stay valid while the group lives; every run recomputes each
+ * problem from the current contents of its buffers. */
+UVATRMM_API int uvatrmm_group_create(uvatrmm_handle_t handle, const uvatrmm_trmm_problem *problems, int count,
+                                    uvatrmm_group_t *group);
+/* Launches the captured graph on the handle's stream (asynchronous; use
+ * uvatrmm_sync for completion and kernel status). */
+UVATRMM_API int uvatrmm_group_run(uvatrmm_group_t group);
+/* Plan facts: total m^2 n (or n^2 m) flops, kernel launches per run, FP64
+ * tiles, Ozaki residue tiles, Ozaki waves, arena bytes. */
+UVATRMM_API int uvatrmm_group_stats(uvatrmm_group_t group, double *flops, int *launches, int64_t *fp64_tiles,
+                                   int64_t *ozaki_tiles, int *ozaki_waves, int64_t *arena_bytes);
+UVATRMM_API int uvatrmm_group_destroy(uvatrmm_group_t group);
+
+/* ---------------------------------------------------------------- autotuner */
+/* The tuned choice for a problem shape: FP64 tier -> output tile edge (64 or
+ * 128); Ozaki tier -> residue-GEMM raster group (4, 8 or 16).  Shapes are
+ * bucketed by (tier, side, ceil(log2 m), ceil(log2 n)); a missing bucket is
+ * measured on the device (when UVATRMM_OPT_AUTOTUNE is 1, the default) and
+ * cached in the file named by $UVATRMM_TUNE_CACHE (default
+ * $HOME/.cache/uvatrmm_tune.txt). */
+UVATRMM_API int uvatrmm_tune(uvatrmm_handle_t handle, int tier, int side, int64_t m, int64_t n, int *choice);
 
 /* Waits for the handle's stream and reports any kernel-side error
  * (UVATRMM_ETIMEOUT for an expired bounded wait). */

@@ -7,6 +7,11 @@ ROOT = os.path.dirname(os.path.dirname(os.path.abspath(__file__)))
 if ROOT not in sys.path:
     sys.path.insert(0, ROOT)
 
+# The autotuner's cache of this test session lives in a private temp file.
+if "UVATRMM_TUNE_CACHE" not in os.environ:
+    import tempfile
+    os.environ["UVATRMM_TUNE_CACHE"] = os.path.join(tempfile.mkdtemp(prefix="uvatrmm_tune_"), "tune.txt")
+
 
 def pytest_configure(config):
     config.addinivalue_line("markers", "gpu: needs a GB300 (sm_103) CUDA device")

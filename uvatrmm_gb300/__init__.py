@@ -131,6 +131,55 @@ class Handle:
         return v.value
 
 
+TIER_FP64, TIER_OZAKI = 0, 1
+
+
+class Group:
+    """A grouped batch of device TRMMs captured in a CUDA graph.
+
+    `problems` is a list of dicts with keys layout, side, uplo, transa, diag,
+    m, n, alpha, A (tensor), lda, B (tensor), ldb, tier, moduli."""
+
+    def __init__(self, handle: "Handle", problems):
+        from ._lib import TrmmProblem
+        arr = (TrmmProblem * max(1, len(problems)))()
+        for i, p in enumerate(problems):
+            arr[i] = TrmmProblem(p["layout"], p["side"], p["uplo"], p["transa"], p["diag"], p["m"], p["n"],
+                                 p.get("alpha", 1.0), _ptr(p["A"]), p["lda"], _ptr(p["B"]), p["ldb"],
+                                 p.get("tier", TIER_FP64), p.get("moduli", 0))
+        g = C.c_void_p()
+        check(lib().uvatrmm_group_create(handle.h, arr, len(problems), C.byref(g)))
+        self.g, self.handle = g, handle
+
+    def run(self) -> None:
+        check(lib().uvatrmm_group_run(self.g))
+
+    def stats(self) -> dict:
+        f, la, wv = C.c_double(), C.c_int(), C.c_int()
+        t64, toz, ab = C.c_int64(), C.c_int64(), C.c_int64()
+        check(lib().uvatrmm_group_stats(self.g, C.byref(f), C.byref(la), C.byref(t64), C.byref(toz), C.byref(wv),
+                                        C.byref(ab)))
+        return {"flops": f.value, "launches": la.value, "fp64_tiles": t64.value, "ozaki_tiles": toz.value,
+                "ozaki_waves": wv.value, "arena_bytes": ab.value}
+
+    def close(self) -> None:
+        if self.g:
+            lib().uvatrmm_group_destroy(self.g)
+            self.g = None
+
+    def __del__(self):
+        try:
+            self.close()
+        except Exception:
+            pass
+
+
+def tune(handle: "Handle", tier: int, side: int, m: int, n: int) -> int:
+    c = C.c_int()
+    check(lib().uvatrmm_tune(handle.h, tier, side, m, n, C.byref(c)))
+    return c.value
+
+
 def ozaki_plan(k: int, moduli: int = 0):
     """(moduli, bits per scaled entry) the Ozaki path uses for inner dimension k."""
     mo, bi = C.c_int(), C.c_int()

@@ -50,6 +50,23 @@ SIGNATURES = {
 }
 
 
+class TrmmProblem(C.Structure):
+    """uvatrmm_trmm_problem (include/uvatrmm.h)."""
+    _fields_ = [("layout", i32), ("side", i32), ("uplo", i32), ("transa", i32), ("diag", i32),
+                ("m", i64), ("n", i64), ("alpha", dbl), ("A", vp), ("lda", i64), ("B", vp), ("ldb", i64),
+                ("tier", i32), ("moduli", i32)]
+
+
+SIGNATURES.update({
+    "uvatrmm_group_create": (i32, [vp, C.POINTER(TrmmProblem), i32, C.POINTER(vp)]),
+    "uvatrmm_group_run": (i32, [vp]),
+    "uvatrmm_group_stats": (i32, [vp, C.POINTER(dbl), C.POINTER(i32), C.POINTER(i64), C.POINTER(i64),
+                                  C.POINTER(i32), C.POINTER(i64)]),
+    "uvatrmm_group_destroy": (i32, [vp]),
+    "uvatrmm_tune": (i32, [vp, i32, i32, i64, i64, C.POINTER(i32)]),
+})
+
+
 class UvatrmmError(RuntimeError):
     def __init__(self, status: int, msg: str):
         super().__init__(f"uvatrmm status {status}: {msg}")

@@ -293,6 +293,10 @@ UVATRMM_API int uvatrmm_set_option(uvatrmm_handle_t h, int option, int value) {
       if (value < 64) break;
       h->ozaki_scratch_mb = value;
       return ok();
+    case UVATRMM_OPT_AUTOTUNE:
+      if (value != 0 && value != 1) break;
+      h->autotune = value != 0;
+      return ok();
     case UVATRMM_OPT_STAGE_TIMING:
       if (value != 0 && value != 1) break;
       if (value && !h->sev[0])

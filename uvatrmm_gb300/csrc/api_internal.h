@@ -18,6 +18,8 @@ struct uvatrmm_handle_st {
   int shape = UVATRMM_SHAPE_TRAPEZOID;
   int tile = 0;
   int64_t ozaki_scratch_mb = 49152;  // residue-plane budget per pass (MiB)
+  bool autotune = true;
+  int oz_raster = 0;  // residue-GEMM raster group of single Ozaki calls (0 = default)
   // Grow-only device workspace slots: 0-2 plain-path staging, 3 reductions,
   // 4 Ozaki scales, 5 Ozaki residue planes, 6 Ozaki product residues,
   // 7 Ozaki error-estimate scratch.
@@ -71,6 +73,15 @@ Trmm normalise(int layout, int side, int uplo, int transa, int diag, int64_t m, 
 int device_trmm(uvatrmm_handle_t h, int layout, int side, int uplo, int transa, int diag, int64_t m, int64_t n,
                 double alpha, const double *dA, int64_t lda, const double *dB, int64_t ldb, double *dC,
                 int64_t ldc, bool in_place, int schedule, int shape);
+
+// Ozaki emulated TRMM on device buffers, in place on dB (ozaki_api.cu).
+int ozaki_device(uvatrmm_handle_t h, int layout, int side, int uplo, int transa, int diag, int64_t m, int64_t n,
+                 double alpha, const double *dA, int64_t lda, double *dB, int64_t ldb, int moduli, double *relerr,
+                 int *bits_out);
+
+// Autotuner (tune.cu): tuned tile edge (FP64) or raster group (Ozaki) for a
+// problem shape; measures and caches a missing bucket when h->autotune.
+int tune_choice(uvatrmm_handle_t h, int tier, int side, int64_t m, int64_t n, int *choice);
 
 // ||X - R||_F / ||R||_F over column-major device blocks.
 int rel_frobenius(uvatrmm_handle_t h, int64_t rows, int64_t cols, const double *X, int64_t ldx, const double *R,

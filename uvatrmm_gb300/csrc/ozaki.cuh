@@ -20,6 +20,7 @@
 // N (the slice count) sets M and hence t; see ozaki_bits().
 #pragma once
 
+#include <cuda.h>
 #include <cuda_runtime.h>
 #include <stdint.h>
 
@@ -71,15 +72,38 @@ int oz_reassemble(const OzPlan &plan, const uint8_t *res, const int *e_row, cons
 // planes LR[l-l0][i][k] (Mp x Kp) and RR[l-l0][j][k] (Np x Kp), writes
 // res[l][j][i] = (sum_k LR*RR) mod m_l.  K range per output tile follows the
 // triangle (tri_left: rows of Lft; else columns of Rgt).
+struct OzGroupProb;
 struct OzGemmLaunch {
   const uint16_t *LR, *RR;
   uint8_t *res;
   int64_t Mp, Np, Kp, M, N, K;
   int l0, l1;
   bool tri_left, tri_lower;
+  int raster_group = 8;          // major tiles per raster group (0 = default)
+  OzGroupProb *desc = nullptr;   // device slot for the descriptor (single launches)
   int *status;
   int num_sms;
 };
 int launch_oz_gemm(const OzGemmLaunch &L, cudaStream_t st, const char **why);
+
+// One residue GEMM of a grouped launch as the device reads it (64-byte
+// aligned; TMA reads the two tensor maps from global memory).
+struct alignas(64) OzGroupProb {
+  CUtensorMap tmA, tmB;
+  int64_t Mp, Np, M, N, K;
+  int l0, l1;
+  int tri_left, tri_lower, grows;
+  int tiles_m, tiles_n, tiles_per_mod, group;
+  uint8_t *res;
+  int64_t plane;
+  int tile_begin, tile_count;
+};
+// Fills the descriptor of one residue GEMM (tile_begin left to the caller).
+int oz_group_prob(const OzGemmLaunch &L, OzGroupProb *out, const char **why);
+// Sets the residue GEMM's launch attributes (call before a stream capture).
+int oz_gemm_prepare();
+// One persistent launch over nprob residue GEMMs (device array sorted by tile_begin).
+int launch_oz_gemm_group(const OzGroupProb *dprobs, int nprob, int total_tiles, int *status, int num_sms,
+                         cudaStream_t st, const char **why);
 
 }  // namespace uvt

@@ -27,6 +27,8 @@ void operands(const Trmm &t, const double *dA, int64_t lda, const double *dB, in
   }
 }
 
+}  // namespace
+
 int ozaki_device(uvatrmm_handle_t h, int layout, int side, int uplo, int transa, int diag, int64_t m, int64_t n,
                  double alpha, const double *dA, int64_t lda, double *dB, int64_t ldb, int moduli, double *relerr,
                  int *bits_out) {
@@ -57,7 +59,8 @@ int ozaki_device(uvatrmm_handle_t h, int layout, int side, int uplo, int transa,
   // Residue planes per modulus: (Mp + Np) x Kp bf16; passes of G moduli.
   const int64_t per_mod = (plan.Mp + plan.Np) * plan.Kp * 2;
   int G = (int)std::max<int64_t>(1, std::min<int64_t>(plan.n_moduli, (h->ozaki_scratch_mb << 20) / per_mod));
-  int *e = static_cast<int *>(workspace(h, 4, (size_t)(plan.Mp + plan.Np) * sizeof(int)));
+  const size_t e_bytes = (size_t)round_up((plan.Mp + plan.Np) * (int64_t)sizeof(int), 256);
+  int *e = static_cast<int *>(workspace(h, 4, e_bytes + sizeof(OzGroupProb)));
   uint8_t *res = static_cast<uint8_t *>(workspace(h, 6, (size_t)plan.n_moduli * plan.Mp * plan.Np));
   uint16_t *planes = static_cast<uint16_t *>(workspace(h, 5, (size_t)G * per_mod));
   if (!e || !res || !planes) return uvatrmm_last_status();
@@ -113,6 +116,8 @@ int ozaki_device(uvatrmm_handle_t h, int layout, int side, int uplo, int transa,
     g.tri_lower = (t.uplo == CblasLower) != (t.trans != 0);
     g.status = h->dctl + 1;
     g.num_sms = h->num_sms;
+    g.desc = reinterpret_cast<OzGroupProb *>(reinterpret_cast<char *>(e) + e_bytes);
+    g.raster_group = h->oz_raster;
     const char *why = nullptr;
     rc = launch_oz_gemm(g, h->stream, &why);
     if (rc != UVATRMM_OK) return fail(rc, why ? why : "residue GEMM launch failed");
@@ -154,7 +159,11 @@ int ozaki_device(uvatrmm_handle_t h, int layout, int side, int uplo, int transa,
   return ok();
 }
 
-}  // namespace
+void ozaki_operands(const Trmm &t, const double *dA, int64_t lda, const double *dB, int64_t ldb, OzOperand &L,
+                    OzOperand &R) {
+  operands(t, dA, lda, dB, ldb, L, R);
+}
+
 }  // namespace uvt
 
 using namespace uvt;

@@ -38,14 +38,10 @@ constexpr size_t SMEM = 1024 + (size_t)STAGES * STAGE_BYTES + 256;
 // (bits 7-9 = 1, 10-12 = 1), both K-major, N/8 at bits 17-22, M/16 at 24-28.
 constexpr uint32_t IDESC = (1u << 4) | (1u << 7) | (1u << 10) | ((uint32_t)(BN >> 3) << 17) | ((uint32_t)(BM >> 4) << 24);
 
+// Launch-wide parameters; the problems themselves are OzGroupProb entries in
+// global memory (their tensor maps are read by TMA from there).
 struct GParams {
-  int64_t Mp, Np, M, N, K;
-  int l0, l1;
-  int tri_left, grows;   // triangle on Lft; work grows with the major index
-  int tri_lower;
-  int tiles_m, tiles_n, tiles_per_mod, total_tiles, group;
-  uint8_t *res;
-  int64_t plane;
+  int nprob, total_tiles;
   int *status;
   float mod_f[kMaxModuli];
   float inv_f[kMaxModuli];
@@ -55,7 +51,24 @@ struct Tile {
   int l, ti, tj, ks0, ks1;
 };
 
-__device__ __forceinline__ Tile decode(const GParams &p, int t) {
+__device__ __forceinline__ void tmap_acquire(const CUtensorMap *m) {
+  asm volatile("fence.proxy.tensormap::generic.acquire.gpu [%0], 128;" ::"l"(reinterpret_cast<uint64_t>(m))
+               : "memory");
+}
+
+// Problem owning global tile t (problems sorted by tile_begin).
+__device__ __forceinline__ int find_problem(const OzGroupProb *probs, int nprob, int t) {
+  int lo = 0, hi = nprob - 1;
+  while (lo < hi) {
+    const int mid = (lo + hi + 1) >> 1;
+    if (probs[mid].tile_begin <= t) lo = mid;
+    else hi = mid - 1;
+  }
+  return lo;
+}
+
+// Local tile t of problem p: modulus, tile coordinates and K slab range.
+__device__ __forceinline__ Tile decode(const OzGroupProb &p, int t) {
   Tile T;
   T.l = p.l0 + t / p.tiles_per_mod;
   int r = t % p.tiles_per_mod;
@@ -147,8 +160,7 @@ __device__ __forceinline__ float mod_pos(float v, float m, float inv) {
 
 // ---------------------------------------------------------------- kernel
 __global__ void __launch_bounds__(NUM_THREADS, 1)
-    oz_gemm_kernel(const __grid_constant__ CUtensorMap tmA, const __grid_constant__ CUtensorMap tmB,
-                   const __grid_constant__ GParams p) {
+    oz_gemm_kernel(const OzGroupProb *__restrict__ probs, const __grid_constant__ GParams p) {
   extern __shared__ uint8_t smem_raw[];
   uint8_t *base = reinterpret_cast<uint8_t *>((reinterpret_cast<uintptr_t>(smem_raw) + 1023) & ~uintptr_t(1023));
   uint64_t *bars = reinterpret_cast<uint64_t *>(base + STAGES * STAGE_BYTES);
@@ -185,15 +197,21 @@ __global__ void __launch_bounds__(NUM_THREADS, 1)
   if (warp == 0) {
     // ------------------------------------------------------------ TMA producer
     if (lane == 0) {
-      tma_prefetch_desc(&tmA);
-      tma_prefetch_desc(&tmB);
       int s = 0;
       uint32_t ph = 0, issued = 0, last_ph[STAGES] = {0, 0, 0, 0};
       bool ok = true;
+      int cur = -1;
       for (int t = blockIdx.x; ok && t < p.total_tiles; t += gridDim.x) {
-        const Tile T = decode(p, t);
-        const int ya = (int)((T.l - p.l0) * p.Mp + (int64_t)T.ti * BM);
-        const int yb = (int)((T.l - p.l0) * p.Np + (int64_t)T.tj * BN);
+        const int pi = find_problem(probs, p.nprob, t);
+        const OzGroupProb &P = probs[pi];
+        if (pi != cur) {
+          tmap_acquire(&P.tmA);
+          tmap_acquire(&P.tmB);
+          cur = pi;
+        }
+        const Tile T = decode(P, t - P.tile_begin);
+        const int ya = (int)((T.l - P.l0) * P.Mp + (int64_t)T.ti * BM);
+        const int yb = (int)((T.l - P.l0) * P.Np + (int64_t)T.tj * BN);
         for (int ks = T.ks0; ks < T.ks1; ++ks) {
           if (!mbar_wait_bounded(&empty[s], ph ^ 1)) {
             record_error(p.status, KERR_WAIT_TIMEOUT);
@@ -201,8 +219,8 @@ __global__ void __launch_bounds__(NUM_THREADS, 1)
             break;
           }
           mbar_arrive_expect_tx(&full[s], STAGE_BYTES);
-          tma_load_2d(smA(s), &tmA, ks * BK, ya, &full[s]);
-          tma_load_2d(smB(s), &tmB, ks * BK, yb, &full[s]);
+          tma_load_2d(smA(s), &P.tmA, ks * BK, ya, &full[s]);
+          tma_load_2d(smB(s), &P.tmB, ks * BK, yb, &full[s]);
           issued |= 1u << s;
           last_ph[s] = ph;
           if (++s == STAGES) { s = 0; ph ^= 1; }
@@ -219,7 +237,8 @@ __global__ void __launch_bounds__(NUM_THREADS, 1)
       uint32_t ph = 0, uses[2] = {0, 0};
       bool ok = true, any = false;
       for (int t = blockIdx.x; ok && t < p.total_tiles; t += gridDim.x) {
-        const Tile T = decode(p, t);
+        const OzGroupProb &P = probs[find_problem(probs, p.nprob, t)];
+        const Tile T = decode(P, t - P.tile_begin);
         const int nslab = T.ks1 - T.ks0;
         const int nchunk = (nslab + CHUNK_SLABS - 1) / CHUNK_SLABS;
         for (int c = 0; ok && c < nchunk; ++c) {
@@ -268,7 +287,8 @@ __global__ void __launch_bounds__(NUM_THREADS, 1)
     uint32_t uses[2] = {0, 0};
     bool ok = true;
     for (int t = blockIdx.x; ok && t < p.total_tiles; t += gridDim.x) {
-      const Tile T = decode(p, t);
+      const OzGroupProb &P = probs[find_problem(probs, p.nprob, t)];
+      const Tile T = decode(P, t - P.tile_begin);
       const int nslab = T.ks1 - T.ks0;
       const int nchunk = (nslab + CHUNK_SLABS - 1) / CHUNK_SLABS;
       const float m = p.mod_f[T.l], inv = p.inv_f[T.l];
@@ -304,7 +324,7 @@ __global__ void __launch_bounds__(NUM_THREADS, 1)
           // Final: residue of (acc[b] + acc[other]) as bytes.
           const bool two = nchunk >= 2;
           const int64_t i = (int64_t)T.ti * BM + row;
-          uint8_t *out = p.res + (int64_t)T.l * p.plane + i;
+          uint8_t *out = P.res + (int64_t)T.l * P.plane + i;
 #pragma unroll 1
           for (int cb = 0; cb < BN / 32; ++cb) {
             uint32_t v[32], w[32];
@@ -319,7 +339,7 @@ __global__ void __launch_bounds__(NUM_THREADS, 1)
                 r += mod_pos(__uint_as_float(w[e]), m, inv);
                 if (r >= m) r -= m;
               }
-              out[(j0 + e) * p.Mp] = (uint8_t)(int)r;
+              out[(j0 + e) * P.Mp] = (uint8_t)(int)r;
             }
           }
           tc_fence_before();
@@ -343,9 +363,13 @@ __global__ void __launch_bounds__(NUM_THREADS, 1)
 
 }  // namespace
 
-int launch_oz_gemm(const OzGemmLaunch &L, cudaStream_t st, const char **why) {
+int oz_group_prob(const OzGemmLaunch &L, OzGroupProb *out, const char **why) {
   *why = nullptr;
-  if (L.l1 <= L.l0 || L.M <= 0 || L.N <= 0 || L.K <= 0) return UVATRMM_OK;
+  memset(out, 0, sizeof(*out));
+  if (L.l1 <= L.l0 || L.M <= 0 || L.N <= 0 || L.K <= 0) {
+    *why = "empty residue GEMM";
+    return UVATRMM_EINVAL;
+  }
   if (L.Mp % BM || L.Np % BN || L.Kp % BK) {
     *why = "residue planes are not padded to the tile sizes";
     return UVATRMM_EINVAL;
@@ -355,47 +379,82 @@ int launch_oz_gemm(const OzGemmLaunch &L, cudaStream_t st, const char **why) {
     *why = "problem too large for one residue pass";
     return UVATRMM_EINVAL;
   }
-  CUtensorMap tmA, tmB;
-  if (make_tmap_2d(&tmA, CU_TENSOR_MAP_DATA_TYPE_BFLOAT16, 2, L.LR, L.Kp, nmod * L.Mp, L.Kp * 2, BK, BM, true) ||
-      make_tmap_2d(&tmB, CU_TENSOR_MAP_DATA_TYPE_BFLOAT16, 2, L.RR, L.Kp, nmod * L.Np, L.Kp * 2, BK, BN, true)) {
+  if (make_tmap_2d(&out->tmA, CU_TENSOR_MAP_DATA_TYPE_BFLOAT16, 2, L.LR, L.Kp, nmod * L.Mp, L.Kp * 2, BK, BM,
+                   true) ||
+      make_tmap_2d(&out->tmB, CU_TENSOR_MAP_DATA_TYPE_BFLOAT16, 2, L.RR, L.Kp, nmod * L.Np, L.Kp * 2, BK, BN,
+                   true)) {
     *why = "tensor map encoding failed for the residue planes";
     return UVATRMM_EDEVICE;
   }
+  out->Mp = L.Mp; out->Np = L.Np; out->M = L.M; out->N = L.N; out->K = L.K;
+  out->l0 = L.l0; out->l1 = L.l1;
+  out->tri_left = L.tri_left;
+  out->tri_lower = L.tri_lower;
+  out->grows = L.tri_left ? L.tri_lower : !L.tri_lower;
+  out->tiles_m = (int)(L.Mp / BM);
+  out->tiles_n = (int)(L.Np / BN);
+  out->tiles_per_mod = out->tiles_m * out->tiles_n;
+  out->tile_count = out->tiles_per_mod * nmod;
+  out->group = L.raster_group > 0 ? L.raster_group : 8;
+  out->res = L.res;
+  out->plane = L.Mp * L.Np;
+  return UVATRMM_OK;
+}
+
+int oz_gemm_prepare() {
+  static bool attr = false;
+  if (!attr) {
+    if (cudaFuncSetAttribute(oz_gemm_kernel, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)SMEM) != cudaSuccess)
+      return UVATRMM_EDEVICE;
+    attr = true;
+  }
+  return UVATRMM_OK;
+}
+
+int launch_oz_gemm_group(const OzGroupProb *dprobs, int nprob, int total_tiles, int *status, int num_sms,
+                         cudaStream_t st, const char **why) {
+  *why = nullptr;
+  if (nprob <= 0 || total_tiles <= 0) return UVATRMM_OK;
   GParams g;
   memset(&g, 0, sizeof(g));
-  g.Mp = L.Mp; g.Np = L.Np; g.M = L.M; g.N = L.N; g.K = L.K;
-  g.l0 = L.l0; g.l1 = L.l1;
-  g.tri_left = L.tri_left;
-  g.tri_lower = L.tri_lower;
-  g.grows = L.tri_left ? L.tri_lower : !L.tri_lower;
-  g.tiles_m = (int)(L.Mp / BM);
-  g.tiles_n = (int)(L.Np / BN);
-  g.tiles_per_mod = g.tiles_m * g.tiles_n;
-  g.total_tiles = g.tiles_per_mod * nmod;
-  g.group = 8;
-  g.res = L.res;
-  g.plane = L.Mp * L.Np;
-  g.status = L.status;
+  g.nprob = nprob;
+  g.total_tiles = total_tiles;
+  g.status = status;
   for (int l = 0; l < kMaxModuli; ++l) {
     g.mod_f[l] = (float)kModuli[l];
     g.inv_f[l] = 1.0f / (float)kModuli[l];
   }
-  static bool attr = false;
-  if (!attr) {
-    if (cudaFuncSetAttribute(oz_gemm_kernel, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)SMEM) != cudaSuccess) {
-      *why = "cannot reserve shared memory for the residue GEMM";
-      return UVATRMM_EDEVICE;
-    }
-    attr = true;
+  if (oz_gemm_prepare() != UVATRMM_OK) {
+    *why = "cannot reserve shared memory for the residue GEMM";
+    return UVATRMM_EDEVICE;
   }
-  const int grid = std::min(L.num_sms, g.total_tiles);
-  oz_gemm_kernel<<<grid, NUM_THREADS, SMEM, st>>>(tmA, tmB, g);
+  const int grid = std::min(num_sms, total_tiles);
+  oz_gemm_kernel<<<grid, NUM_THREADS, SMEM, st>>>(dprobs, g);
   cudaError_t e = cudaGetLastError();
   if (e != cudaSuccess) {
     *why = cudaGetErrorString(e);
     return UVATRMM_EDEVICE;
   }
   return UVATRMM_OK;
+}
+
+int launch_oz_gemm(const OzGemmLaunch &L, cudaStream_t st, const char **why) {
+  *why = nullptr;
+  if (L.l1 <= L.l0 || L.M <= 0 || L.N <= 0 || L.K <= 0) return UVATRMM_OK;
+  if (!L.desc) {
+    *why = "no device slot for the residue GEMM descriptor";
+    return UVATRMM_EINVAL;
+  }
+  OzGroupProb hp;
+  if (int rc = oz_group_prob(L, &hp, why)) return rc;
+  hp.tile_begin = 0;
+  // A pageable-source async copy stages the descriptor before returning.
+  cudaError_t e = cudaMemcpyAsync(L.desc, &hp, sizeof(hp), cudaMemcpyHostToDevice, st);
+  if (e != cudaSuccess) {
+    *why = cudaGetErrorString(e);
+    return UVATRMM_EDEVICE;
+  }
+  return launch_oz_gemm_group(L.desc, 1, hp.tile_count, L.status, L.num_sms, st, why);
 }
 
 }  // namespace uvt

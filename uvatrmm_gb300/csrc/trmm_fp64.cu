@@ -46,15 +46,12 @@ enum : int { SF_FIRST = 1, SF_LAST = 2 };
 
 struct StageInfo {
   int ti, tj, kt, flags;  // ti < 0 marks the end of the work
+  int prob;               // problem of a grouped launch (0 otherwise)
+  int pad[3];
 };
 
-struct KParams {
-  int64_t M, N, K, ldc;
-  double alpha;
-  double *C;
+struct KParams : TileProb {
   int *counter, *status;
-  int tri_left, tri_lower, unit, trapezoid;
-  int n_major, n_minor, major_rev;  // tiles along the triangular dimension / the other one
   int sched_static, Q, CP;
   int qb[kMaxBlocks + 1];  // work-rank bounds of the Q major blocks
   int cb[kMaxBlocks + 1];  // bounds of the CP minor panels
@@ -104,7 +101,7 @@ __device__ __forceinline__ double tri_select(double v, int cls, int unit) {
   return cls == 0 ? 0.0 : (cls == 2 && unit ? 1.0 : v);
 }
 
-__device__ __forceinline__ void tile_kslabs(const KParams &p, int ti, int tj, int BM, int &kt0, int &kt1) {
+__device__ __forceinline__ void tile_kslabs(const TileProb &p, int ti, int tj, int BM, int &kt0, int &kt1) {
   int64_t kb, ke;
   if (p.tri_left) {
     int64_t i0 = (int64_t)ti * BM;
@@ -119,7 +116,7 @@ __device__ __forceinline__ void tile_kslabs(const KParams &p, int ti, int tj, in
   kt1 = (int)((ke + kBK - 1) / kBK);
 }
 
-__device__ __forceinline__ void decode_major(const KParams &p, int r, int minor, int &ti, int &tj) {
+__device__ __forceinline__ void decode_major(const TileProb &p, int r, int minor, int &ti, int &tj) {
   int major = p.major_rev ? (p.n_major - 1 - r) : r;
   if (p.tri_left) { ti = major; tj = minor; }
   else { ti = minor; tj = major; }
@@ -127,7 +124,9 @@ __device__ __forceinline__ void decode_major(const KParams &p, int r, int minor,
 
 // ---------------------------------------------------------------- DFMA engine
 // Thread (tx, ty) owns rows ty + TY*ii and columns tx + 16*jj of the tile.
-template <int BM, bool LK, bool RK>
+// The slab layouts (LK, RK) are template arguments of the slab functions, so
+// one engine (one set of accumulator registers) serves every layout.
+template <int BM>
 struct DfmaEngine {
   using C = Cfg<BM>;
   double acc[C::TM][C::TN];
@@ -140,6 +139,7 @@ struct DfmaEngine {
 #pragma unroll
       for (int jj = 0; jj < C::TN; ++jj) acc[ii][jj] = 0.0;
   }
+  template <bool LK, bool RK>
   __device__ void slab(const double *Ls, const double *Rs) {
 #pragma unroll
     for (int k = 0; k < kBK; ++k) {
@@ -156,7 +156,8 @@ struct DfmaEngine {
   }
   // Diagonal slab `s` (k in [16s, 16s+16) of the tile's diagonal block,
   // whose rows and columns share the same origin).
-  __device__ void slab_diag(const double *Ls, const double *Rs, int s, const KParams &p) {
+  template <bool LK, bool RK>
+  __device__ void slab_diag(const double *Ls, const double *Rs, int s, const TileProb &p) {
     const bool trap = p.trapezoid, lower = p.tri_lower, unit = p.unit;
     const int c0 = 16 * s;
 #pragma unroll 1
@@ -193,7 +194,7 @@ struct DfmaEngine {
       }
     }
   }
-  __device__ void store(const KParams &p, int64_t i0, int64_t j0) {
+  __device__ void store(const TileProb &p, int64_t i0, int64_t j0) {
 #pragma unroll
     for (int jj = 0; jj < C::TN; ++jj) {
       int64_t j = j0 + tx + 16 * jj;
@@ -214,7 +215,7 @@ __device__ __forceinline__ void dmma884(double &c0, double &c1, double a, double
                : "d"(a), "d"(b));
 }
 
-template <int BM, bool LK, bool RK>
+template <int BM>
 struct DmmaEngine {
   using C = Cfg<BM>;
   // Warp grid (NCW/4) rows x 4 columns; warp tile WM x WN in m8n8 fragments.
@@ -236,6 +237,7 @@ struct DmmaEngine {
 #pragma unroll
       for (int h = 0; h < FN; ++h) acc[f][h][0] = acc[f][h][1] = 0.0;
   }
+  template <bool LK, bool RK>
   __device__ void slab(const double *Ls, const double *Rs) {
 #pragma unroll
     for (int k = 0; k < kBK; k += 4) {
@@ -250,7 +252,8 @@ struct DmmaEngine {
         for (int h = 0; h < FN; ++h) dmma884(acc[f][h][0], acc[f][h][1], a[f], b[h]);
     }
   }
-  __device__ void slab_diag(const double *Ls, const double *Rs, int s, const KParams &p) {
+  template <bool LK, bool RK>
+  __device__ void slab_diag(const double *Ls, const double *Rs, int s, const TileProb &p) {
     const bool trap = p.trapezoid, lower = p.tri_lower, unit = p.unit;
 #pragma unroll 1
     for (int k = 0; k < kBK; k += 4) {
@@ -283,7 +286,7 @@ struct DmmaEngine {
       }
     }
   }
-  __device__ void store(const KParams &p, int64_t i0, int64_t j0) {
+  __device__ void store(const TileProb &p, int64_t i0, int64_t j0) {
 #pragma unroll
     for (int f = 0; f < FM; ++f)
 #pragma unroll
@@ -299,7 +302,7 @@ struct DmmaEngine {
 };
 
 // ---------------------------------------------------------------- kernel
-template <int BM, bool LK, bool RK, template <int, bool, bool> class EngineT>
+template <int BM, bool LK, bool RK, template <int> class EngineT>
 __global__ void __launch_bounds__(Cfg<BM>::THREADS, Cfg<BM>::MIN_BLOCKS)
     trmm_fp64_kernel(const __grid_constant__ CUtensorMap tmL, const __grid_constant__ CUtensorMap tmR,
                      const __grid_constant__ KParams p) {
@@ -348,7 +351,7 @@ __global__ void __launch_bounds__(Cfg<BM>::THREADS, Cfg<BM>::MIN_BLOCKS)
         const int i0 = ti * BM, j0 = tj * C::BN;
         for (int kt = kt0; kt < kt1; ++kt) {
           if (!claim()) return false;
-          info[s] = StageInfo{ti, tj, kt, (kt == kt0 ? SF_FIRST : 0) | (kt == kt1 - 1 ? SF_LAST : 0)};
+          info[s] = StageInfo{ti, tj, kt, (kt == kt0 ? SF_FIRST : 0) | (kt == kt1 - 1 ? SF_LAST : 0), 0, {}};
           mbar_arrive_expect_tx(&full[s], C::STAGE_BYTES);
           const int k0 = kt * kBK;
           if constexpr (LK) tma_load_2d(Lst(s), &tmL, k0, i0, &full[s]);
@@ -381,7 +384,7 @@ __global__ void __launch_bounds__(Cfg<BM>::THREADS, Cfg<BM>::MIN_BLOCKS)
       }
       // End-of-work marker (a plain arrive completes the phase).
       if (claim()) {
-        info[s] = StageInfo{-1, -1, 0, 0};
+        info[s] = StageInfo{-1, -1, 0, 0, 0, {}};
         mbar_arrive(&full[s]);
         issued |= 1u << s;
         last_ph[s] = ph;
@@ -393,7 +396,7 @@ __global__ void __launch_bounds__(Cfg<BM>::THREADS, Cfg<BM>::MIN_BLOCKS)
     }
   } else {
     // ------------------------------------------------------------ consumers
-    EngineT<BM, LK, RK> eng;
+    EngineT<BM> eng;
     eng.init(threadIdx.x);
     int s = 0;
     uint32_t ph = 0;
@@ -410,9 +413,9 @@ __global__ void __launch_bounds__(Cfg<BM>::THREADS, Cfg<BM>::MIN_BLOCKS)
       const int64_t k0 = (int64_t)inf.kt * kBK;
       const int64_t d0 = p.tri_left ? i0 : j0;
       if (k0 >= d0 && k0 < d0 + BM)
-        eng.slab_diag(Lst(s), Rst(s), (int)((k0 - d0) / kBK), p);
+        eng.template slab_diag<LK, RK>(Lst(s), Rst(s), (int)((k0 - d0) / kBK), p);
       else
-        eng.slab(Lst(s), Rst(s));
+        eng.template slab<LK, RK>(Lst(s), Rst(s));
       __syncwarp();
       if (lane == 0) mbar_arrive(&empty[s]);
       if (inf.flags & SF_LAST) eng.store(p, i0, j0);
@@ -422,7 +425,146 @@ __global__ void __launch_bounds__(Cfg<BM>::THREADS, Cfg<BM>::MIN_BLOCKS)
   __syncthreads();
 }
 
-template <int BM, bool LK, bool RK, template <int, bool, bool> class EngineT>
+// ---------------------------------------------------------------- grouped kernel
+// Many TRMMs in one persistent launch: the problems' tiles form one list
+// (problem p owns tiles [tile_begin, tile_begin + tile_count)), pulled from
+// an atomic counter; inside a problem, longest tiles first.  Each problem
+// carries its own tensor maps (in global memory) and slab layouts, which
+// the consumers dispatch on at run time.
+__device__ __forceinline__ void tmap_acquire(const CUtensorMap *m) {
+  asm volatile("fence.proxy.tensormap::generic.acquire.gpu [%0], 128;" ::"l"(reinterpret_cast<uint64_t>(m))
+               : "memory");
+}
+
+__device__ __forceinline__ int find_problem(const Fp64GroupProb *probs, int nprob, int t) {
+  int lo = 0, hi = nprob - 1;
+  while (lo < hi) {
+    const int mid = (lo + hi + 1) >> 1;
+    if (probs[mid].tile_begin <= t) lo = mid;
+    else hi = mid - 1;
+  }
+  return lo;
+}
+
+template <int BM, template <int> class EngineT>
+__global__ void __launch_bounds__(Cfg<BM>::THREADS, Cfg<BM>::MIN_BLOCKS)
+    trmm_fp64_group_kernel(const Fp64GroupProb *__restrict__ probs, int nprob, int total_tiles, int *counter,
+                           int *status) {
+  using C = Cfg<BM>;
+  extern __shared__ uint8_t smem_raw[];
+  uint8_t *base = reinterpret_cast<uint8_t *>((reinterpret_cast<uintptr_t>(smem_raw) + 1023) & ~uintptr_t(1023));
+  uint64_t *full = reinterpret_cast<uint64_t *>(base + C::STAGES * C::STAGE_BYTES);
+  uint64_t *empty = full + C::STAGES;
+  StageInfo *info = reinterpret_cast<StageInfo *>(empty + C::STAGES);
+  auto Lst = [&](int s) { return reinterpret_cast<double *>(base + s * C::STAGE_BYTES); };
+  auto Rst = [&](int s) { return reinterpret_cast<double *>(base + s * C::STAGE_BYTES) + C::L_ELEMS; };
+
+  const int warp = threadIdx.x >> 5, lane = threadIdx.x & 31;
+  if (threadIdx.x == 0) {
+    for (int s = 0; s < C::STAGES; ++s) {
+      mbar_init(&full[s], 1);
+      mbar_init(&empty[s], C::NCW);
+    }
+    fence_barrier_init();
+  }
+  __syncthreads();
+
+  if (warp == C::NCW) {
+    if (lane == 0) {
+      int s = 0;
+      uint32_t ph = 0, issued = 0;
+      uint32_t last_ph[C::STAGES];
+      bool ok = true;
+      while (ok) {
+        const int t = atomicAdd(counter, 1);
+        if (t >= total_tiles) break;
+        const int pi = find_problem(probs, nprob, t);
+        const Fp64GroupProb &P = probs[pi];
+        const TileProb tp = P.tp;
+        const int r = t - P.tile_begin;
+        int ti, tj, kt0, kt1;
+        decode_major(tp, tp.n_major - 1 - r / tp.n_minor, r % tp.n_minor, ti, tj);
+        tile_kslabs(tp, ti, tj, BM, kt0, kt1);
+        tmap_acquire(&P.tmL);
+        tmap_acquire(&P.tmR);
+        const int i0 = ti * BM, j0 = tj * C::BN;
+        for (int kt = kt0; kt < kt1; ++kt) {
+          if (!mbar_wait_bounded(&empty[s], ph ^ 1)) {
+            record_error(status, KERR_WAIT_TIMEOUT);
+            ok = false;
+            break;
+          }
+          info[s] = StageInfo{ti, tj, kt, (kt == kt0 ? SF_FIRST : 0) | (kt == kt1 - 1 ? SF_LAST : 0), pi, {}};
+          mbar_arrive_expect_tx(&full[s], C::STAGE_BYTES);
+          const int k0 = kt * kBK;
+          if (P.lk) tma_load_2d(Lst(s), &P.tmL, k0, i0, &full[s]);
+          else tma_load_2d(Lst(s), &P.tmL, i0, k0, &full[s]);
+          if (P.rk) tma_load_2d(Rst(s), &P.tmR, k0, j0, &full[s]);
+          else tma_load_2d(Rst(s), &P.tmR, j0, k0, &full[s]);
+          issued |= 1u << s;
+          last_ph[s] = ph;
+          if (++s == C::STAGES) { s = 0; ph ^= 1; }
+        }
+      }
+      if (mbar_wait_bounded(&empty[s], ph ^ 1)) {
+        info[s] = StageInfo{-1, -1, 0, 0, 0, {}};
+        mbar_arrive(&full[s]);
+        issued |= 1u << s;
+        last_ph[s] = ph;
+      } else {
+        record_error(status, KERR_WAIT_TIMEOUT);
+      }
+      for (int st = 0; st < C::STAGES; ++st)
+        if ((issued >> st) & 1u)
+          if (!mbar_wait_bounded(&full[st], last_ph[st])) record_error(status, KERR_WAIT_TIMEOUT);
+    }
+  } else {
+    EngineT<BM> eng;
+    eng.init(threadIdx.x);
+    int s = 0;
+    uint32_t ph = 0;
+    while (true) {
+      if (!mbar_wait_bounded(&full[s], ph)) {
+        record_error(status, KERR_WAIT_TIMEOUT);
+        break;
+      }
+      const volatile StageInfo *vi = &info[s];
+      const StageInfo inf{vi->ti, vi->tj, vi->kt, vi->flags, vi->prob, {}};
+      if (inf.ti < 0) break;
+      const Fp64GroupProb &P = probs[inf.prob];
+      const TileProb tp = P.tp;
+      if (inf.flags & SF_FIRST) eng.zero();
+      const int64_t i0 = (int64_t)inf.ti * BM, j0 = (int64_t)inf.tj * C::BN;
+      const int64_t k0 = (int64_t)inf.kt * kBK;
+      const int64_t d0 = tp.tri_left ? i0 : j0;
+      const double *Ls = Lst(s), *Rs = Rst(s);
+      const int lay = (P.lk ? 2 : 0) | (P.rk ? 1 : 0);
+      if (k0 >= d0 && k0 < d0 + BM) {
+        const int sd = (int)((k0 - d0) / kBK);
+        switch (lay) {
+          case 3: eng.template slab_diag<true, true>(Ls, Rs, sd, tp); break;
+          case 2: eng.template slab_diag<true, false>(Ls, Rs, sd, tp); break;
+          case 1: eng.template slab_diag<false, true>(Ls, Rs, sd, tp); break;
+          default: eng.template slab_diag<false, false>(Ls, Rs, sd, tp); break;
+        }
+      } else {
+        switch (lay) {
+          case 3: eng.template slab<true, true>(Ls, Rs); break;
+          case 2: eng.template slab<true, false>(Ls, Rs); break;
+          case 1: eng.template slab<false, true>(Ls, Rs); break;
+          default: eng.template slab<false, false>(Ls, Rs); break;
+        }
+      }
+      __syncwarp();
+      if (lane == 0) mbar_arrive(&empty[s]);
+      if (inf.flags & SF_LAST) eng.store(tp, i0, j0);
+      if (++s == C::STAGES) { s = 0; ph ^= 1; }
+    }
+  }
+  __syncthreads();
+}
+
+template <int BM, bool LK, bool RK, template <int> class EngineT>
 int launch_variant(const CUtensorMap &tmL, const CUtensorMap &tmR, const KParams &kp, int grid,
                    cudaStream_t stream) {
   auto kern = trmm_fp64_kernel<BM, LK, RK, EngineT>;
@@ -437,7 +579,7 @@ int launch_variant(const CUtensorMap &tmL, const CUtensorMap &tmR, const KParams
   return cudaGetLastError() == cudaSuccess ? UVATRMM_OK : UVATRMM_EDEVICE;
 }
 
-template <int BM, template <int, bool, bool> class EngineT>
+template <int BM, template <int> class EngineT>
 int dispatch_layout(bool lk, bool rk, const CUtensorMap &tmL, const CUtensorMap &tmR, const KParams &kp, int grid,
                     cudaStream_t st) {
   if (lk && rk) return launch_variant<BM, true, true, EngineT>(tmL, tmR, kp, grid, st);
@@ -540,6 +682,92 @@ int launch_trmm_fp64(const Fp64Launch &L, cudaStream_t stream, const char **why)
   }
   if (BM == 128) return dispatch_layout<128, DfmaEngine>(lk, rk, tmL, tmR, kp, grid, stream);
   return dispatch_layout<64, DfmaEngine>(lk, rk, tmL, tmR, kp, grid, stream);
+}
+
+int fp64_group_prob(const Fp64Launch &L, int BM, Fp64GroupProb *out, const char **why) {
+  *why = nullptr;
+  memset(out, 0, sizeof(*out));
+  if (BM != 64 && BM != 128) {
+    *why = "tile must be 64 or 128";
+    return UVATRMM_EINVAL;
+  }
+  if (L.M <= 0 || L.N <= 0 || L.K <= 0 || L.M > INT32_MAX / 2 || L.N > INT32_MAX / 2 || L.K > INT32_MAX / 2) {
+    *why = "dimension out of range for a grouped problem";
+    return UVATRMM_EINVAL;
+  }
+  const uint32_t boxL_in = L.lft_kmajor ? kBK : BM, boxL_out = L.lft_kmajor ? BM : kBK;
+  const uint32_t boxR_in = L.rgt_kmajor ? kBK : BM, boxR_out = L.rgt_kmajor ? BM : kBK;
+  if (make_tmap_2d(&out->tmL, CU_TENSOR_MAP_DATA_TYPE_FLOAT64, 8, L.xl.ptr, L.xl.rows, L.xl.cols, L.xl.ld * 8,
+                   boxL_in, boxL_out, L.lft_kmajor) ||
+      make_tmap_2d(&out->tmR, CU_TENSOR_MAP_DATA_TYPE_FLOAT64, 8, L.xr.ptr, L.xr.rows, L.xr.cols, L.xr.ld * 8,
+                   boxR_in, boxR_out, L.rgt_kmajor)) {
+    *why = "tensor map encoding failed (alignment or driver)";
+    return UVATRMM_EDEVICE;
+  }
+  TileProb &tp = out->tp;
+  tp.M = L.M; tp.N = L.N; tp.K = L.K; tp.ldc = L.ldc;
+  tp.alpha = L.alpha; tp.C = L.C;
+  tp.tri_left = L.tri_left; tp.tri_lower = L.tri_lower; tp.unit = L.unit;
+  tp.trapezoid = L.shape == UVATRMM_SHAPE_TRAPEZOID;
+  const int tiles_m = (int)((L.M + BM - 1) / BM), tiles_n = (int)((L.N + BM - 1) / BM);
+  tp.n_major = L.tri_left ? tiles_m : tiles_n;
+  tp.n_minor = L.tri_left ? tiles_n : tiles_m;
+  const bool grows = L.tri_left ? L.tri_lower : !L.tri_lower;
+  tp.major_rev = grows ? 0 : 1;
+  out->lk = L.lft_kmajor;
+  out->rk = L.rgt_kmajor;
+  out->tile_count = tiles_m * tiles_n;
+  return UVATRMM_OK;
+}
+
+namespace {
+template <int BM, template <int> class EngineT>
+int group_attr() {
+  static bool attr_set = false;
+  if (!attr_set) {
+    if (cudaFuncSetAttribute(trmm_fp64_group_kernel<BM, EngineT>, cudaFuncAttributeMaxDynamicSharedMemorySize,
+                             (int)Cfg<BM>::SMEM) != cudaSuccess)
+      return UVATRMM_EDEVICE;
+    attr_set = true;
+  }
+  return UVATRMM_OK;
+}
+
+template <int BM, template <int> class EngineT>
+int launch_group_variant(const Fp64GroupProb *dprobs, int nprob, int total, int *counter, int *status, int grid,
+                         cudaStream_t st) {
+  if (int rc = group_attr<BM, EngineT>()) return rc;
+  trmm_fp64_group_kernel<BM, EngineT><<<grid, Cfg<BM>::THREADS, Cfg<BM>::SMEM, st>>>(dprobs, nprob, total, counter,
+                                                                                      status);
+  return cudaGetLastError() == cudaSuccess ? UVATRMM_OK : UVATRMM_EDEVICE;
+}
+}  // namespace
+
+int fp64_group_prepare(int BM, int engine) {
+  if (engine == UVATRMM_ENGINE_DMMA) return BM == 128 ? group_attr<128, DmmaEngine>() : group_attr<64, DmmaEngine>();
+  return BM == 128 ? group_attr<128, DfmaEngine>() : group_attr<64, DfmaEngine>();
+}
+
+int launch_trmm_fp64_group(const Fp64GroupProb *dprobs, int nprob, int total_tiles, int BM, int engine,
+                           int *counter, int *status, int num_sms, cudaStream_t st, const char **why) {
+  *why = nullptr;
+  if (nprob <= 0 || total_tiles <= 0) return UVATRMM_OK;
+  if (BM != 64 && BM != 128) {
+    *why = "tile must be 64 or 128";
+    return UVATRMM_EINVAL;
+  }
+  if (cudaMemsetAsync(counter, 0, sizeof(int), st) != cudaSuccess) return UVATRMM_EDEVICE;
+  const int per_sm = BM == 128 ? Cfg<128>::MIN_BLOCKS : Cfg<64>::MIN_BLOCKS;
+  const int grid = std::min(num_sms * per_sm, total_tiles);
+  int rc;
+  if (engine == UVATRMM_ENGINE_DMMA)
+    rc = BM == 128 ? launch_group_variant<128, DmmaEngine>(dprobs, nprob, total_tiles, counter, status, grid, st)
+                   : launch_group_variant<64, DmmaEngine>(dprobs, nprob, total_tiles, counter, status, grid, st);
+  else
+    rc = BM == 128 ? launch_group_variant<128, DfmaEngine>(dprobs, nprob, total_tiles, counter, status, grid, st)
+                   : launch_group_variant<64, DfmaEngine>(dprobs, nprob, total_tiles, counter, status, grid, st);
+  if (rc != UVATRMM_OK) *why = "grouped FP64 kernel launch failed";
+  return rc;
 }
 
 }  // namespace uvt

@@ -1,6 +1,7 @@
 // Plain FP64 TRMM: launch descriptor shared by the kernel file and the API.
 #pragma once
 
+#include <cuda.h>
 #include <cuda_runtime.h>
 #include <stdint.h>
 
@@ -40,6 +41,33 @@ struct Fp64Launch {
 
 // Enqueues the kernel on `stream`.  Returns a uvatrmm_status.
 int launch_trmm_fp64(const Fp64Launch &L, cudaStream_t stream, const char **why);
+
+// What the kernel's tile walk, engines and epilogue need about one problem.
+struct TileProb {
+  int64_t M, N, K, ldc;
+  double alpha;
+  double *C;
+  int tri_left, tri_lower, unit, trapezoid;
+  int n_major, n_minor, major_rev;  // tiles along the triangular dimension / the other one
+};
+
+// One problem of a grouped launch, as the device reads it (64-byte aligned:
+// the tensor maps are read by TMA from global memory).
+struct alignas(64) Fp64GroupProb {
+  CUtensorMap tmL, tmR;
+  TileProb tp;
+  int lk, rk;
+  int tile_begin, tile_count;
+};
+
+// Fills `out` for problem L with tile edge BM (tile_begin left to the caller).
+int fp64_group_prob(const Fp64Launch &L, int BM, Fp64GroupProb *out, const char **why);
+// Sets the grouped kernel's launch attributes (call before a stream capture).
+int fp64_group_prepare(int BM, int engine);
+// One persistent launch over `nprob` problems (device array `dprobs`, sorted
+// by tile_begin, tiles [0, total_tiles)); `counter` is zeroed here.
+int launch_trmm_fp64_group(const Fp64GroupProb *dprobs, int nprob, int total_tiles, int BM, int engine,
+                           int *counter, int *status, int num_sms, cudaStream_t stream, const char **why);
 
 // Tile edge the automatic choice picks for this problem.
 int fp64_auto_tile(int64_t M, int64_t N, int64_t K, int num_sms);
