@@ -250,7 +250,87 @@ def run_gpu(args, ws, rank, local):
     del hA, hB, hB0
     if not args.no_ozaki:
         out["ozaki"] = run_ozaki(args, h, dev, stream, rank, achieved)
+    if args.batch > 0:
+        hb = u.Handle(stream=stream)  # its own workspace for the one-call-per-problem comparison
+        out["batch"] = run_batch(args, hb, dev, stream)
+        hb.close()
     return out
+
+
+def batch_problems(count, seed, dev, h):
+    """The batching configuration: m log-uniform [64, 4096], n log-uniform
+    [16, 4096], side/uplo/trans uniform, 70 % FP64 / 30 % Ozaki, entries
+    uniform[-1,1), seed 3 (sizes drawn with numpy's PCG64 from the seed)."""
+    import numpy as np
+    import torch
+
+    import uvatrmm_gb300 as u
+    rng = np.random.default_rng(seed)
+    probs = []
+    for i in range(count):
+        m = int(round(np.exp(rng.uniform(np.log(64), np.log(4096)))))
+        n = int(round(np.exp(rng.uniform(np.log(16), np.log(4096)))))
+        side = [u.LEFT, u.RIGHT][rng.integers(2)]
+        uplo = [u.LOWER, u.UPPER][rng.integers(2)]
+        trans = [u.NOTRANS, u.TRANS][rng.integers(2)]
+        tier = u.TIER_OZAKI if rng.random() < 0.3 else u.TIER_FP64
+        ka = m if side == u.LEFT else n
+        A = torch.empty(ka * ka, dtype=torch.float64, device=dev)
+        B = torch.empty(m * n, dtype=torch.float64, device=dev)
+        h.gen_uniform(seed, 2 * i, ka, ka, A, 1, ka)
+        h.gen_uniform(seed, 2 * i + 1, m, n, B, 1, m)
+        probs.append(dict(layout=u.COL, side=side, uplo=uplo, transa=trans, diag=u.NONUNIT, m=m, n=n, alpha=1.0,
+                          A=A, lda=ka, B=B, ldb=m, tier=tier, moduli=0))
+    h.sync()
+    return probs
+
+
+def run_batch(args, h, dev, stream):
+    """Grouped persistent launches in one CUDA graph vs one call per problem."""
+    import torch
+
+    import uvatrmm_gb300 as u
+    probs = batch_problems(args.batch, 3, dev, h)
+    t0 = time.perf_counter()
+    g = u.Group(h, probs)
+    plan_s = time.perf_counter() - t0
+    st = g.stats()
+    g.run()  # warm-up
+    h.sync()
+    times = []
+    for _ in range(args.batch_steps):
+        e0, e1 = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
+        e0.record(stream)
+        g.run()
+        e1.record(stream)
+        h.sync()
+        times.append(e0.elapsed_time(e1))
+    ms = statistics.mean(times)
+    # The same problems one call at a time (FP64: uvatrmm_dtrmm_device; Ozaki: uvatrmm_ozaki_dtrmm_device).
+    e0, e1 = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
+    e0.record(stream)
+    for p in probs:
+        a = (p["layout"], p["side"], p["uplo"], p["transa"], p["diag"], p["m"], p["n"], 1.0, p["A"], p["lda"],
+             p["B"], p["ldb"])
+        if p["tier"] == u.TIER_OZAKI:
+            h.ozaki_device(*a)
+        else:
+            h.dtrmm_device(*a)
+    e1.record(stream)
+    h.sync()
+    seq_ms = e0.elapsed_time(e1)
+    g.close()
+    n_oz = sum(p["tier"] == u.TIER_OZAKI for p in probs)
+    del probs
+    torch.cuda.empty_cache()
+    return {"workload": f"{args.batch} TRMMs, m logU[64,4096], n logU[16,4096], side/uplo/trans uniform, "
+                        f"{args.batch - n_oz} FP64 + {n_oz} Ozaki, seed 3",
+            "value": round(st["flops"] / (ms * 1e-3) / 1e12, 4), "unit": "TFLOP/s (sum of m^2 n)",
+            "ms_per_batch": round(ms, 3), "runs": len(times), "graph_kernel_launches": st["launches"],
+            "fp64_tiles": st["fp64_tiles"], "ozaki_tiles": st["ozaki_tiles"], "ozaki_waves": st["ozaki_waves"],
+            "arena_gib": round(st["arena_bytes"] / 2 ** 30, 2), "plan_and_capture_s": round(plan_s, 2),
+            "one_call_per_problem_ms": round(seq_ms, 3),
+            "speedup_vs_one_call_per_problem": round(seq_ms / ms, 3)}
 
 
 def bf16_peak():
@@ -374,6 +454,8 @@ def main():
     ap.add_argument("--no-ozaki", action="store_true")
     ap.add_argument("--ozaki-n", type=int, default=32768)
     ap.add_argument("--ozaki-steps", type=int, default=3)
+    ap.add_argument("--batch", type=int, default=2000)
+    ap.add_argument("--batch-steps", type=int, default=2)
     args = ap.parse_args()
     ws, rank, local = dist_env()
     threads = os.cpu_count() or 1
