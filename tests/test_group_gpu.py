@@ -13,7 +13,7 @@ from tests.helpers import COL, LEFT, LOWER, NONUNIT, NOTRANS, RIGHT, ROW, TRANS,
 pytestmark = pytest.mark.gpu
 
 
-def mixed_problems(count, seed, max_dim=600):
+def mixed_problems(count, seed, max_dim=600, min_dim=8):
     import torch
     rng = np.random.default_rng(seed)
     out = []
@@ -23,8 +23,8 @@ def mixed_problems(count, seed, max_dim=600):
         uplo = [LOWER, UPPER][rng.integers(2)]
         trans = [NOTRANS, TRANS][rng.integers(2)]
         diag = [NONUNIT, UNIT][rng.integers(2)]
-        m = int(np.exp(rng.uniform(np.log(8), np.log(max_dim))))
-        n = int(np.exp(rng.uniform(np.log(4), np.log(max_dim))))
+        m = int(np.exp(rng.uniform(np.log(min_dim), np.log(max_dim))))
+        n = int(np.exp(rng.uniform(np.log(max(4, min_dim // 2)), np.log(max_dim))))
         tier = u.TIER_OZAKI if rng.random() < 0.3 else u.TIER_FP64
         A, lda, B, ldb = make_problem(layout, side, uplo, m, n, lda_pad=int(rng.integers(2)),
                                       ldb_pad=int(rng.integers(3)), seed=seed * 1000 + i)
@@ -75,7 +75,8 @@ def test_group_matches_single_calls_bitwise(handle):
 
 def test_group_ozaki_waves_under_a_small_budget(handle):
     import torch
-    probs = [dict(p, tier=u.TIER_OZAKI) for p in mixed_problems(12, seed=5, max_dim=400)]
+    # each problem needs > 64 MiB of residue planes at these sizes
+    probs = [dict(p, tier=u.TIER_OZAKI) for p in mixed_problems(5, seed=5, max_dim=1100, min_dim=800)]
     refs = [single_reference(handle, p) for p in probs]
     u.check(u.lib().uvatrmm_set_option(handle.h, 5, 64))  # 64 MiB of Ozaki scratch per wave
     try:

@@ -219,8 +219,11 @@ int build(uvatrmm_group_t g, const uvatrmm_trmm_problem *probs, int count) {
     waves.back().push_back(i);
     max_wave = std::max(max_wave, wave_bytes);
   }
-  std::vector<size_t> off_wdesc(waves.size());
-  for (size_t w = 0; w < waves.size(); ++w) off_wdesc[w] = A.take(waves[w].size() * sizeof(OzGroupProb), 64);
+  std::vector<size_t> off_wdesc(waves.size()), off_wtab(waves.size());
+  for (size_t w = 0; w < waves.size(); ++w) {
+    off_wdesc[w] = A.take(waves[w].size() * sizeof(OzGroupProb), 64);
+    off_wtab[w] = A.take(oz_wave_table_bytes((int)waves[w].size()));
+  }
   const size_t off_wave = A.take(max_wave);
   g->arena_bytes = A.used;
   cudaError_t e = cudaMalloc(&g->arena, std::max<size_t>(g->arena_bytes, 256));
@@ -255,12 +258,25 @@ int build(uvatrmm_group_t g, const uvatrmm_trmm_problem *probs, int count) {
     if (int rc = fp64_group_prepare(classes[c], UVATRMM_ENGINE_DFMA)) return fail(rc, "FP64 kernel attributes");
   }
   std::vector<int> wave_total(waves.size(), 0);
+  std::vector<OzWaveTables> wave_tab(waves.size());
   for (size_t w = 0; w < waves.size(); ++w) {
     std::vector<OzGroupProb> hd(waves[w].size());
+    std::vector<OzWaveItem> items(waves[w].size());
     int begin = 0;
     for (size_t k = 0; k < waves[w].size(); ++k) {
       const OzItem &it = oz[waves[w][k]];
       const OzPlan &pl = it.plan;
+      OzWaveItem &wi = items[k];
+      ozaki_operands(it.t, it.A, it.lda, it.B, it.ldb, wi.L, wi.R);
+      wi.e_row = reinterpret_cast<int *>(base + off_wave + it.offE);
+      wi.e_col = wi.e_row + pl.Mp;
+      wi.plan = pl;
+      wi.LR = reinterpret_cast<uint16_t *>(base + off_wave + it.offP);
+      wi.RR = wi.LR + (int64_t)pl.n_moduli * pl.Mp * pl.Kp;
+      wi.res = reinterpret_cast<uint8_t *>(base + off_wave + it.offR);
+      wi.alpha = it.t.alpha;
+      wi.C = it.B;
+      wi.ldc = it.ldb;
       OzGemmLaunch L;
       L.LR = reinterpret_cast<uint16_t *>(base + off_wave + it.offP);
       L.RR = L.LR + (int64_t)pl.n_moduli * pl.Mp * pl.Kp;
@@ -280,6 +296,8 @@ int build(uvatrmm_group_t g, const uvatrmm_trmm_problem *probs, int count) {
     g->oz_tiles += begin;
     e = cudaMemcpy(base + off_wdesc[w], hd.data(), hd.size() * sizeof(OzGroupProb), cudaMemcpyHostToDevice);
     if (e != cudaSuccess) return cuda_fail(e, "Ozaki descriptors");
+    if (int rc = oz_wave_tables(items.data(), (int)items.size(), base + off_wtab[w], &wave_tab[w]))
+      return fail(rc, "Ozaki wave job tables");
   }
   if (!waves.empty())
     if (int rc = oz_gemm_prepare()) return fail(rc, "residue GEMM attributes");
@@ -303,33 +321,15 @@ int build(uvatrmm_group_t g, const uvatrmm_trmm_problem *probs, int count) {
     if (cudaMemset2DAsync(zeros[z].first, zero_ld[z] * 8, 0, zeros[z].second.m * 8, zeros[z].second.n, st) !=
         cudaSuccess)
       rc = UVATRMM_EDEVICE;
+  // Per wave: grouped scales + residues (2 launches), one grouped residue
+  // GEMM, one grouped reassembly.
   for (size_t w = 0; w < waves.size() && rc == UVATRMM_OK; ++w) {
-    for (int i : waves[w]) {
-      const OzItem &it = oz[i];
-      OzOperand L, R;
-      ozaki_operands(it.t, it.A, it.lda, it.B, it.ldb, L, R);
-      int *e_row = reinterpret_cast<int *>(base + off_wave + it.offE), *e_col = e_row + it.plan.Mp;
-      uint16_t *LR = reinterpret_cast<uint16_t *>(base + off_wave + it.offP);
-      uint16_t *RR = LR + (int64_t)it.plan.n_moduli * it.plan.Mp * it.plan.Kp;
-      rc = oz_scales(L, e_row, st);
-      if (rc == UVATRMM_OK) rc = oz_scales(R, e_col, st);
-      if (rc == UVATRMM_OK) rc = oz_residues(L, e_row, it.plan.bits, 0, it.plan.n_moduli, it.plan.Mp, it.plan.Kp, LR, st);
-      if (rc == UVATRMM_OK) rc = oz_residues(R, e_col, it.plan.bits, 0, it.plan.n_moduli, it.plan.Np, it.plan.Kp, RR, st);
-      if (rc != UVATRMM_OK) break;
-      g->launches += 4;
-    }
-    if (rc != UVATRMM_OK) break;
-    rc = launch_oz_gemm_group(reinterpret_cast<OzGroupProb *>(base + off_wdesc[w]), (int)waves[w].size(),
-                              wave_total[w], h->dctl + 1, h->num_sms, st, &why);
-    g->launches += 1;
-    for (int i : waves[w]) {
-      if (rc != UVATRMM_OK) break;
-      const OzItem &it = oz[i];
-      int *e_row = reinterpret_cast<int *>(base + off_wave + it.offE), *e_col = e_row + it.plan.Mp;
-      rc = oz_reassemble(it.plan, reinterpret_cast<uint8_t *>(base + off_wave + it.offR), e_row, e_col,
-                         it.t.alpha, it.B, it.ldb, st);
-      g->launches += 1;
-    }
+    rc = oz_wave_prep(wave_tab[w], st);
+    if (rc == UVATRMM_OK)
+      rc = launch_oz_gemm_group(reinterpret_cast<OzGroupProb *>(base + off_wdesc[w]), (int)waves[w].size(),
+                                wave_total[w], h->dctl + 1, h->num_sms, st, &why);
+    if (rc == UVATRMM_OK) rc = oz_wave_reassemble(wave_tab[w], st);
+    g->launches += 4;
   }
   for (auto &it : f64) {
     if (rc != UVATRMM_OK) break;

@@ -68,6 +68,30 @@ int oz_residues(const OzOperand &op, const int *e, int bits, int l0, int l1, int
 int oz_reassemble(const OzPlan &plan, const uint8_t *res, const int *e_row, const int *e_col, double alpha,
                   double *C, int64_t ldc, cudaStream_t st);
 
+// Grouped slicing and reassembly for a wave of problems (one launch per
+// stage): scales (each block covers all of K, so no prior fill), residue
+// planes of all moduli, and the CRT reassembly into C.
+struct OzWaveItem {
+  OzOperand L, R;
+  int *e_row, *e_col;
+  OzPlan plan;
+  uint16_t *LR, *RR;
+  const uint8_t *res;
+  double alpha;
+  double *C;
+  int64_t ldc;
+};
+struct OzWaveTables {
+  void *scale, *resid, *crt;
+  int n_scale, n_resid, n_crt;
+  int64_t b_scale, b_resid, b_crt;
+};
+size_t oz_wave_table_bytes(int nitems);
+// Builds the job tables of `n` items into device memory `dev` (synchronous copies).
+int oz_wave_tables(const OzWaveItem *items, int n, void *dev, OzWaveTables *out);
+int oz_wave_prep(const OzWaveTables &t, cudaStream_t st);
+int oz_wave_reassemble(const OzWaveTables &t, cudaStream_t st);
+
 // The tcgen05 residue GEMM (ozaki_gemm.cu): for moduli [l0, l1), with residue
 // planes LR[l-l0][i][k] (Mp x Kp) and RR[l-l0][j][k] (Np x Kp), writes
 // res[l][j][i] = (sum_k LR*RR) mod m_l.  K range per output tile follows the

@@ -5,6 +5,7 @@
 #include <algorithm>
 #include <cmath>
 #include <cstring>
+#include <vector>
 
 #include "api_internal.h"
 #include "common.cuh"
@@ -39,13 +40,17 @@ __device__ __forceinline__ int exp_above(double v) {
 // Tiles of 32 (p) x 64 (k) per 256-thread block; grid.y splits K.
 constexpr int TP = 32, TK = 64;
 
-__global__ void __launch_bounds__(256) scale_kernel(OzOperand op, int *e, int64_t k_per_block) {
+// Rows [32 bx, 32 bx + 32) of the operand over k in [by * kpb, (by+1) * kpb):
+// the maximum exponent per row.  `direct`: this block covers all of K, so it
+// writes e[p] itself (no prior fill, no atomics across blocks).
+__device__ __forceinline__ void scale_body(const OzOperand &op, int *e, int64_t bx, int64_t by, int64_t k_per_block,
+                                           bool direct) {
   __shared__ int red[TP];
   const int tid = threadIdx.x;
   if (tid < TP) red[tid] = kExpNone;
   __syncthreads();
-  const int64_t p0 = (int64_t)blockIdx.x * TP;
-  const int64_t kb = (int64_t)blockIdx.y * k_per_block, ke = min(op.K, kb + k_per_block);
+  const int64_t p0 = bx * TP;
+  const int64_t kb = by * k_per_block, ke = min(op.K, kb + k_per_block);
   int best = kExpNone;
   int myp;
   if (op.kcontig) {
@@ -73,7 +78,14 @@ __global__ void __launch_bounds__(256) scale_kernel(OzOperand op, int *e, int64_
   }
   (void)myp;
   __syncthreads();
-  if (tid < TP && p0 + tid < op.P && red[tid] != kExpNone) atomicMax(&e[p0 + tid], red[tid]);
+  if (tid < TP && p0 + tid < op.P) {
+    if (direct) e[p0 + tid] = red[tid];
+    else if (red[tid] != kExpNone) atomicMax(&e[p0 + tid], red[tid]);
+  }
+}
+
+__global__ void __launch_bounds__(256) scale_kernel(OzOperand op, int *e, int64_t k_per_block) {
+  scale_body(op, e, blockIdx.x, blockIdx.y, k_per_block, false);
 }
 
 // ---------------------------------------------------------------- residues
@@ -104,11 +116,12 @@ __device__ __forceinline__ void store_residues(const uint32_t (&w)[4], bool neg,
   }
 }
 
-__global__ void __launch_bounds__(256) residue_kernel(OzOperand op, const int *e, int bits, int l0, int l1,
-                                                      int64_t Pp, int64_t Kp, uint16_t *R) {
+// The 32 (p) x 64 (k) residue tile (bx = k tile, by = p tile).
+__device__ __forceinline__ void residue_body(const OzOperand &op, const int *e, int bits, int l0, int l1, int64_t Pp,
+                                             int64_t Kp, uint16_t *R, int64_t bx, int64_t by) {
   __shared__ double tile[TP][TK + 1];
   const int tid = threadIdx.x;
-  const int64_t p0 = (int64_t)blockIdx.y * TP, k0 = (int64_t)blockIdx.x * TK;
+  const int64_t p0 = by * TP, k0 = bx * TK;
   // Load (coalesced along the contiguous dimension of X).
   for (int idx = tid; idx < TP * TK; idx += 256) {
     int pp, kk;
@@ -143,6 +156,11 @@ __global__ void __launch_bounds__(256) residue_kernel(OzOperand op, const int *e
   }
 }
 
+__global__ void __launch_bounds__(256) residue_kernel(OzOperand op, const int *e, int bits, int l0, int l1,
+                                                      int64_t Pp, int64_t Kp, uint16_t *R) {
+  residue_body(op, e, bits, l0, l1, Pp, Kp, R, blockIdx.x, blockIdx.y);
+}
+
 // ---------------------------------------------------------------- reassembly
 struct CrtConst {
   int n;
@@ -174,14 +192,15 @@ __device__ __forceinline__ void add3(uint64_t a[3], const uint64_t b[3]) {
   a[2] = a[2] + b[2] + (uint64_t)(t >> 64);
 }
 
-__global__ void __launch_bounds__(256) reassemble_kernel(const __grid_constant__ CrtConst cc, const uint8_t *res,
-                                                         int64_t Mp, int64_t plane, int64_t M, int64_t N,
-                                                         const int *e_row, const int *e_col, double alpha,
-                                                         double *C, int64_t ldc) {
-  const int64_t i = (int64_t)blockIdx.x * blockDim.x + threadIdx.x;
+// Rows [256 bx, 256 bx + 256) of columns j0, j0 + jstep, ... of C.
+__device__ __forceinline__ void reassemble_body(const CrtConst &cc, const uint8_t *res, int64_t Mp, int64_t plane,
+                                                int64_t M, int64_t N, const int *e_row, const int *e_col,
+                                                double alpha, double *C, int64_t ldc, int64_t bx, int64_t j0,
+                                                int64_t jstep) {
+  const int64_t i = bx * blockDim.x + threadIdx.x;
   if (i >= M) return;
   const int er = e_row[i];
-  for (int64_t j = blockIdx.y; j < N; j += gridDim.y) {
+  for (int64_t j = j0; j < N; j += jstep) {
   const int ec = e_col[j];
   if (er == kExpNone || ec == kExpNone) {
     C[i + j * ldc] = alpha * 0.0;
@@ -243,6 +262,82 @@ __global__ void __launch_bounds__(256) reassemble_kernel(const __grid_constant__
   d = ldexp(d, shift + er + ec - 2 * cc.bits);
   C[i + j * ldc] = alpha * (neg ? -d : d);
   }
+}
+
+__global__ void __launch_bounds__(256) reassemble_kernel(const __grid_constant__ CrtConst cc, const uint8_t *res,
+                                                         int64_t Mp, int64_t plane, int64_t M, int64_t N,
+                                                         const int *e_row, const int *e_col, double alpha,
+                                                         double *C, int64_t ldc) {
+  reassemble_body(cc, res, Mp, plane, M, N, e_row, e_col, alpha, C, ldc, blockIdx.x, blockIdx.y, gridDim.y);
+}
+
+// ---------------------------------------------------------------- grouped (wave) kernels
+// One launch per stage for all problems of a wave: block b belongs to the
+// job whose [block_begin, block_begin + blocks) holds it.
+struct ScaleJob {
+  OzOperand op;
+  int *e;
+  int64_t block_begin;
+};
+struct ResidueJob {
+  OzOperand op;
+  const int *e;
+  int bits, nmod;
+  int64_t Pp, Kp, gx;
+  uint16_t *R;
+  int64_t block_begin;
+};
+struct CrtJob {
+  CrtConst cc;
+  const uint8_t *res;
+  int64_t Mp, plane, M, N, gx;
+  const int *e_row, *e_col;
+  double alpha;
+  double *C;
+  int64_t ldc;
+  int64_t block_begin;
+};
+
+template <class J>
+__device__ __forceinline__ int find_job(const J *jobs, int n, int64_t b) {
+  int lo = 0, hi = n - 1;
+  while (lo < hi) {
+    const int mid = (lo + hi + 1) >> 1;
+    if (jobs[mid].block_begin <= b) lo = mid;
+    else hi = mid - 1;
+  }
+  return lo;
+}
+
+__device__ __forceinline__ int64_t flat_block() { return (int64_t)blockIdx.y * gridDim.x + blockIdx.x; }
+
+__global__ void __launch_bounds__(256) scale_wave_kernel(const ScaleJob *jobs, int n, int64_t total) {
+  const int64_t b = flat_block();
+  if (b >= total) return;
+  const ScaleJob &J = jobs[find_job(jobs, n, b)];
+  scale_body(J.op, J.e, b - J.block_begin, 0, J.op.K, true);
+}
+
+__global__ void __launch_bounds__(256) residue_wave_kernel(const ResidueJob *jobs, int n, int64_t total) {
+  const int64_t b = flat_block();
+  if (b >= total) return;
+  const ResidueJob &J = jobs[find_job(jobs, n, b)];
+  const int64_t lb = b - J.block_begin;
+  residue_body(J.op, J.e, J.bits, 0, J.nmod, J.Pp, J.Kp, J.R, lb % J.gx, lb / J.gx);
+}
+
+__global__ void __launch_bounds__(256) reassemble_wave_kernel(const CrtJob *jobs, int n, int64_t total) {
+  const int64_t b = flat_block();
+  if (b >= total) return;
+  const CrtJob &J = jobs[find_job(jobs, n, b)];
+  const int64_t lb = b - J.block_begin;
+  reassemble_body(J.cc, J.res, J.Mp, J.plane, J.M, J.N, J.e_row, J.e_col, J.alpha, J.C, J.ldc, lb % J.gx, lb / J.gx,
+                  J.N);
+}
+
+dim3 flat_grid(int64_t total) {
+  const int64_t gx = std::min<int64_t>(total, 1 << 20);
+  return dim3((unsigned)std::max<int64_t>(gx, 1), (unsigned)((total + gx - 1) / std::max<int64_t>(gx, 1)));
 }
 
 // ---------------------------------------------------------------- host bigint helpers
@@ -331,8 +426,9 @@ int oz_residues(const OzOperand &op, const int *e, int bits, int l0, int l1, int
   return cudaGetLastError() == cudaSuccess ? UVATRMM_OK : UVATRMM_EDEVICE;
 }
 
-int oz_reassemble(const OzPlan &plan, const uint8_t *res, const int *e_row, const int *e_col, double alpha,
-                  double *C, int64_t ldc, cudaStream_t st) {
+namespace {
+// CRT constants for the first n moduli: W_l = (M/m_l) * ((M/m_l)^-1 mod m_l).
+CrtConst make_crt(const OzPlan &plan) {
   CrtConst cc;
   memset(&cc, 0, sizeof(cc));
   cc.n = plan.n_moduli;
@@ -354,6 +450,87 @@ int oz_reassemble(const OzPlan &plan, const uint8_t *res, const int *e_row, cons
     cc.halfM[k] = half.w[k];
   }
   cc.Mf = (float)((double)M.w[2] + (double)M.w[1] * 0x1p-64 + (double)M.w[0] * 0x1p-128);
+  return cc;
+}
+}  // namespace
+
+size_t oz_wave_table_bytes(int nitems) {
+  auto r = [](size_t b) { return (b + 255) / 256 * 256; };
+  return r(2 * (size_t)nitems * sizeof(ScaleJob)) + r(2 * (size_t)nitems * sizeof(ResidueJob)) +
+         r((size_t)nitems * sizeof(CrtJob));
+}
+
+int oz_wave_tables(const OzWaveItem *items, int n, void *dev, OzWaveTables *out) {
+  std::vector<ScaleJob> sj(2 * n);
+  std::vector<ResidueJob> rj(2 * n);
+  std::vector<CrtJob> cj(n);
+  int64_t bs = 0, br = 0, bc = 0;
+  for (int i = 0; i < n; ++i) {
+    const OzWaveItem &it = items[i];
+    const OzPlan &pl = it.plan;
+    for (int s = 0; s < 2; ++s) {
+      const OzOperand &op = s ? it.R : it.L;
+      sj[2 * i + s] = ScaleJob{op, s ? it.e_col : it.e_row, bs};
+      bs += (op.P + TP - 1) / TP;
+      const int64_t Pp = s ? pl.Np : pl.Mp;
+      const int64_t gx = pl.Kp / TK;
+      rj[2 * i + s] = ResidueJob{op, s ? it.e_col : it.e_row, pl.bits, pl.n_moduli, Pp, pl.Kp, gx,
+                                 s ? it.RR : it.LR, br};
+      br += gx * (Pp / TP);
+    }
+    CrtJob &c = cj[i];
+    c.cc = make_crt(pl);
+    c.res = it.res;
+    c.Mp = pl.Mp;
+    c.plane = pl.Mp * pl.Np;
+    c.M = pl.M;
+    c.N = pl.N;
+    c.gx = (pl.M + 255) / 256;
+    c.e_row = it.e_row;
+    c.e_col = it.e_col;
+    c.alpha = it.alpha;
+    c.C = it.C;
+    c.ldc = it.ldc;
+    c.block_begin = bc;
+    bc += c.gx * pl.N;
+  }
+  auto r = [](size_t b) { return (b + 255) / 256 * 256; };
+  char *base = static_cast<char *>(dev);
+  out->scale = base;
+  out->resid = base + r(sj.size() * sizeof(ScaleJob));
+  out->crt = static_cast<char *>(out->resid) + r(rj.size() * sizeof(ResidueJob));
+  out->n_scale = out->n_resid = 2 * n;
+  out->n_crt = n;
+  out->b_scale = bs;
+  out->b_resid = br;
+  out->b_crt = bc;
+  if (cudaMemcpy(out->scale, sj.data(), sj.size() * sizeof(ScaleJob), cudaMemcpyHostToDevice) != cudaSuccess ||
+      cudaMemcpy(out->resid, rj.data(), rj.size() * sizeof(ResidueJob), cudaMemcpyHostToDevice) != cudaSuccess ||
+      cudaMemcpy(out->crt, cj.data(), cj.size() * sizeof(CrtJob), cudaMemcpyHostToDevice) != cudaSuccess)
+    return UVATRMM_EDEVICE;
+  return UVATRMM_OK;
+}
+
+int oz_wave_prep(const OzWaveTables &t, cudaStream_t st) {
+  if (t.b_scale > 0)
+    scale_wave_kernel<<<flat_grid(t.b_scale), 256, 0, st>>>(static_cast<const ScaleJob *>(t.scale), t.n_scale,
+                                                            t.b_scale);
+  if (t.b_resid > 0)
+    residue_wave_kernel<<<flat_grid(t.b_resid), 256, 0, st>>>(static_cast<const ResidueJob *>(t.resid), t.n_resid,
+                                                              t.b_resid);
+  return cudaGetLastError() == cudaSuccess ? UVATRMM_OK : UVATRMM_EDEVICE;
+}
+
+int oz_wave_reassemble(const OzWaveTables &t, cudaStream_t st) {
+  if (t.b_crt > 0)
+    reassemble_wave_kernel<<<flat_grid(t.b_crt), 256, 0, st>>>(static_cast<const CrtJob *>(t.crt), t.n_crt,
+                                                               t.b_crt);
+  return cudaGetLastError() == cudaSuccess ? UVATRMM_OK : UVATRMM_EDEVICE;
+}
+
+int oz_reassemble(const OzPlan &plan, const uint8_t *res, const int *e_row, const int *e_col, double alpha,
+                  double *C, int64_t ldc, cudaStream_t st) {
+  const CrtConst cc = make_crt(plan);
   if (plan.M <= 0 || plan.N <= 0) return UVATRMM_OK;
   dim3 grid((unsigned)((plan.M + 255) / 256), (unsigned)std::min<int64_t>(plan.N, 65535));
   reassemble_kernel<<<grid, 256, 0, st>>>(cc, res, plan.Mp, plan.Mp * plan.Np, plan.M, plan.N, e_row, e_col,
