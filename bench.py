@@ -254,7 +254,91 @@ def run_gpu(args, ws, rank, local):
         hb = u.Handle(stream=stream)  # its own workspace for the one-call-per-problem comparison
         out["batch"] = run_batch(args, hb, dev, stream)
         hb.close()
+    if args.serve > 0:
+        hs = u.Handle(stream=stream)
+        out["serving"] = run_serving(args, hs, dev, stream)
+        hs.close()
     return out
+
+
+def serve_requests(count, seed, dev, h):
+    """The serving configuration's request mix: m log-uniform [128, 8192], n
+    log-uniform [32, 8192], half exact FP64 / half <= 1e-14 Ozaki, side /
+    uplo / trans uniform, entries uniform[-1,1), seed 4."""
+    import numpy as np
+    import torch
+
+    import uvatrmm_gb300 as u
+    rng = np.random.default_rng(seed)
+    reqs = []
+    for i in range(count):
+        m = int(round(np.exp(rng.uniform(np.log(128), np.log(8192)))))
+        n = int(round(np.exp(rng.uniform(np.log(32), np.log(8192)))))
+        side = [u.LEFT, u.RIGHT][rng.integers(2)]
+        uplo = [u.LOWER, u.UPPER][rng.integers(2)]
+        trans = [u.NOTRANS, u.TRANS][rng.integers(2)]
+        tier = u.TIER_OZAKI if rng.random() < 0.5 else u.TIER_FP64
+        ka = m if side == u.LEFT else n
+        A = torch.empty(ka * ka, dtype=torch.float64, device=dev)
+        B = torch.empty(m * n, dtype=torch.float64, device=dev)
+        h.gen_uniform(seed, 2 * i, ka, ka, A, 1, ka)
+        h.gen_uniform(seed, 2 * i + 1, m, n, B, 1, m)
+        reqs.append(dict(layout=u.COL, side=side, uplo=uplo, transa=trans, diag=u.NONUNIT, m=m, n=n, alpha=1.0,
+                         A=A, lda=ka, B=B, ldb=m, tier=tier, moduli=0))
+    h.sync()
+    return reqs, rng
+
+
+def run_serving(args, h, dev, stream):
+    """Poisson arrivals into the server (device-resident operands, 120 GB
+    budget) at each rate; p50/p99 latency and sustained TFLOP/s, beside the
+    same requests run one at a time through the direct entry points."""
+    import numpy as np
+    import torch
+
+    import uvatrmm_gb300 as u
+    reqs, rng = serve_requests(args.serve, 4, dev, h)
+    flops = [(p["m"] ** 2 * p["n"] if p["side"] == u.LEFT else p["n"] ** 2 * p["m"]) for p in reqs]
+    # one at a time through the direct entry points (the unbatched reference point)
+    alone_ms = []
+    for p in reqs[: min(len(reqs), 200)]:
+        a = (p["layout"], p["side"], p["uplo"], p["transa"], p["diag"], p["m"], p["n"], 1.0, p["A"], p["lda"],
+             p["B"], p["ldb"])
+        t0 = time.perf_counter()
+        (h.ozaki_device if p["tier"] == u.TIER_OZAKI else h.dtrmm_device)(*a)
+        h.sync()
+        alone_ms.append((time.perf_counter() - t0) * 1e3)
+    rates = []
+    for rate in args.serve_rates:
+        srv = u.Server(h, hbm_budget_bytes=int(120e9))
+        gaps = rng.exponential(1.0 / rate, size=len(reqs))
+        ids = []
+        t_next = time.perf_counter()
+        for p, gap in zip(reqs, gaps):
+            t_next += gap
+            while True:
+                d = t_next - time.perf_counter()
+                if d <= 0:
+                    break
+                time.sleep(min(d, 0.001) if d > 0.0002 else 0)
+            ids.append(srv.submit(p))
+        bad = sum(srv.wait(r) != 0 for r in ids)
+        st = srv.stats()
+        srv.close()
+        span = st["last_done_s"] - st["first_submit_s"]
+        rates.append({"rate_req_per_s": rate, "requests": len(ids), "failed": bad,
+                      "p50_ms": round(st["p50_ms"], 3), "p99_ms": round(st["p99_ms"], 3),
+                      "mean_ms": round(st["mean_ms"], 3), "max_ms": round(st["max_ms"], 3),
+                      "sustained_tflops": round(st["served_flops"] / span / 1e12, 4), "ticks": st["ticks"],
+                      "peak_pool_gib": round(st["peak_bytes"] / 2 ** 30, 2)})
+    del reqs
+    torch.cuda.empty_cache()
+    return {"workload": f"{args.serve} requests per rate, m logU[128,8192], n logU[32,8192], 50% FP64 / 50% "
+                        "Ozaki (<=1e-14), Poisson arrivals, 120 GB budget, device-resident operands, seed 4",
+            "alone_p50_ms": round(float(np.percentile(alone_ms, 50)), 3),
+            "alone_p99_ms": round(float(np.percentile(alone_ms, 99)), 3),
+            "alone_requests": len(alone_ms),
+            "total_gflop_per_pass": round(sum(flops) / 1e9, 1), "rates": rates}
 
 
 def batch_problems(count, seed, dev, h):
@@ -456,6 +540,8 @@ def main():
     ap.add_argument("--ozaki-steps", type=int, default=3)
     ap.add_argument("--batch", type=int, default=2000)
     ap.add_argument("--batch-steps", type=int, default=2)
+    ap.add_argument("--serve", type=int, default=300)
+    ap.add_argument("--serve-rates", type=float, nargs="*", default=[100.0, 1000.0, 5000.0])
     args = ap.parse_args()
     ws, rank, local = dist_env()
     threads = os.cpu_count() or 1

@@ -205,6 +205,48 @@ UVATRMM_API int uvatrmm_group_stats(uvatrmm_group_t group, double *flops, int *l
                                    int64_t *ozaki_tiles, int *ozaki_waves, int64_t *arena_bytes);
 UVATRMM_API int uvatrmm_group_destroy(uvatrmm_group_t group);
 
+/* ---------------------------------------------------------------- serving */
+/* No counterpart in the reference.  A request loop with continuous
+ * batching: a server thread admits submitted TRMMs (FIFO) as slots and
+ * device memory under the HBM budget free up, and runs "ticks": grouped
+ * launches over tile ranges taken from every active request, so requests
+ * that arrive while others run join the next tick and share the device
+ * with them.  Each output tile is computed whole inside one launch, so a
+ * result is bitwise the same alone and in any mix. */
+typedef struct uvatrmm_server_st *uvatrmm_server_t;
+typedef struct {
+  int64_t hbm_budget_bytes; /* device memory for admitted requests' working buffers (default 120e9) */
+  int max_active;           /* requests admitted at once (default 512) */
+  double tick_fp64_gflop;   /* FP64-tier work per tick (default 12) */
+  double tick_ozaki_gflop;  /* bf16 residue-GEMM work per tick (default 3000) */
+} uvatrmm_server_config;
+typedef struct {
+  int64_t submitted, completed, failed, cancelled, refused, ticks;
+  double p50_ms, p99_ms, mean_ms, max_ms; /* submit -> result ready, completed requests */
+  double served_flops;                    /* sum of m^2 n (side L) / n^2 m (side R) completed */
+  double first_submit_s, last_done_s;     /* monotonic seconds */
+  int64_t peak_bytes;                     /* largest pool use */
+} uvatrmm_server_stats;
+/* cfg may be NULL (defaults).  The server has its own streams on the
+ * handle's device; the handle is only read at creation. */
+UVATRMM_API int uvatrmm_server_create(uvatrmm_handle_t handle, const uvatrmm_server_config *cfg,
+                                     uvatrmm_server_t *server);
+/* Queues one TRMM and returns its id at once.  operands_on_device != 0: A
+ * and B are device pointers that must stay valid (B receives the result);
+ * else host pointers, copied in at admission and the result copied back
+ * into B.  A request whose working set exceeds the whole budget is refused
+ * (UVATRMM_EBUSY). */
+UVATRMM_API int uvatrmm_server_submit(uvatrmm_server_t server, const uvatrmm_trmm_problem *problem,
+                                     int operands_on_device, int64_t *id);
+/* Waits up to timeout_s (< 0: forever) for request `id`: UVATRMM_OK when its
+ * result is in B, UVATRMM_ENOTREADY on timeout, or the request's error. */
+UVATRMM_API int uvatrmm_server_wait(uvatrmm_server_t server, int64_t id, double timeout_s);
+/* Withdraws a request that has not been admitted yet. */
+UVATRMM_API int uvatrmm_server_cancel(uvatrmm_server_t server, int64_t id);
+UVATRMM_API int uvatrmm_server_get_stats(uvatrmm_server_t server, uvatrmm_server_stats *stats);
+/* Finishes every queued request, then stops the server thread. */
+UVATRMM_API int uvatrmm_server_destroy(uvatrmm_server_t server);
+
 /* ---------------------------------------------------------------- autotuner */
 /* The tuned choice for a problem shape: FP64 tier -> output tile edge (64 or
  * 128); Ozaki tier -> residue-GEMM raster group (4, 8 or 16).  Shapes are

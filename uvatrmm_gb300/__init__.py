@@ -174,6 +174,54 @@ class Group:
             pass
 
 
+def _problem(p):
+    from ._lib import TrmmProblem
+    return TrmmProblem(p["layout"], p["side"], p["uplo"], p["transa"], p["diag"], p["m"], p["n"],
+                       p.get("alpha", 1.0), _ptr(p["A"]), p["lda"], _ptr(p["B"]), p["ldb"],
+                       p.get("tier", TIER_FP64), p.get("moduli", 0))
+
+
+class Server:
+    """The request loop with continuous batching (uvatrmm_server_*)."""
+
+    def __init__(self, handle: "Handle", hbm_budget_bytes=0, max_active=0, tick_fp64_gflop=0.0,
+                 tick_ozaki_gflop=0.0):
+        from ._lib import ServerConfig
+        cfg = ServerConfig(int(hbm_budget_bytes), int(max_active), float(tick_fp64_gflop), float(tick_ozaki_gflop))
+        s = C.c_void_p()
+        check(lib().uvatrmm_server_create(handle.h, C.byref(cfg), C.byref(s)))
+        self.s = s
+
+    def submit(self, problem: dict, on_device: bool = True) -> int:
+        rid = C.c_int64()
+        pr = _problem(problem)
+        check(lib().uvatrmm_server_submit(self.s, C.byref(pr), int(on_device), C.byref(rid)))
+        return rid.value
+
+    def wait(self, rid: int, timeout_s: float = -1.0) -> int:
+        return lib().uvatrmm_server_wait(self.s, rid, timeout_s)
+
+    def cancel(self, rid: int) -> int:
+        return lib().uvatrmm_server_cancel(self.s, rid)
+
+    def stats(self) -> dict:
+        from ._lib import ServerStats
+        st = ServerStats()
+        check(lib().uvatrmm_server_get_stats(self.s, C.byref(st)))
+        return {k: getattr(st, k) for k, _ in ServerStats._fields_}
+
+    def close(self) -> None:
+        if self.s:
+            lib().uvatrmm_server_destroy(self.s)
+            self.s = None
+
+    def __del__(self):
+        try:
+            self.close()
+        except Exception:
+            pass
+
+
 def tune(handle: "Handle", tier: int, side: int, m: int, n: int) -> int:
     c = C.c_int()
     check(lib().uvatrmm_tune(handle.h, tier, side, m, n, C.byref(c)))

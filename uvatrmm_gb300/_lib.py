@@ -57,7 +57,26 @@ class TrmmProblem(C.Structure):
                 ("tier", i32), ("moduli", i32)]
 
 
+class ServerConfig(C.Structure):
+    """uvatrmm_server_config (include/uvatrmm.h)."""
+    _fields_ = [("hbm_budget_bytes", i64), ("max_active", i32), ("tick_fp64_gflop", dbl),
+                ("tick_ozaki_gflop", dbl)]
+
+
+class ServerStats(C.Structure):
+    """uvatrmm_server_stats (include/uvatrmm.h)."""
+    _fields_ = [("submitted", i64), ("completed", i64), ("failed", i64), ("cancelled", i64), ("refused", i64),
+                ("ticks", i64), ("p50_ms", dbl), ("p99_ms", dbl), ("mean_ms", dbl), ("max_ms", dbl),
+                ("served_flops", dbl), ("first_submit_s", dbl), ("last_done_s", dbl), ("peak_bytes", i64)]
+
+
 SIGNATURES.update({
+    "uvatrmm_server_create": (i32, [vp, C.POINTER(ServerConfig), C.POINTER(vp)]),
+    "uvatrmm_server_submit": (i32, [vp, C.POINTER(TrmmProblem), i32, C.POINTER(i64)]),
+    "uvatrmm_server_wait": (i32, [vp, i64, dbl]),
+    "uvatrmm_server_cancel": (i32, [vp, i64]),
+    "uvatrmm_server_get_stats": (i32, [vp, C.POINTER(ServerStats)]),
+    "uvatrmm_server_destroy": (i32, [vp]),
     "uvatrmm_group_create": (i32, [vp, C.POINTER(TrmmProblem), i32, C.POINTER(vp)]),
     "uvatrmm_group_run": (i32, [vp]),
     "uvatrmm_group_stats": (i32, [vp, C.POINTER(dbl), C.POINTER(i32), C.POINTER(i64), C.POINTER(i64),

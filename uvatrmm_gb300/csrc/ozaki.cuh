@@ -24,6 +24,8 @@
 #include <cuda_runtime.h>
 #include <stdint.h>
 
+#include <vector>
+
 namespace uvt {
 
 constexpr int kMaxModuli = 20;
@@ -89,6 +91,9 @@ struct OzWaveTables {
 size_t oz_wave_table_bytes(int nitems);
 // Builds the job tables of `n` items into device memory `dev` (synchronous copies).
 int oz_wave_tables(const OzWaveItem *items, int n, void *dev, OzWaveTables *out);
+// The same tables as a host image (oz_wave_table_bytes(n) bytes) that the
+// caller copies to `dev`; `out` already points into `dev`.
+void oz_wave_image(const OzWaveItem *items, int n, void *dev, std::vector<char> &image, OzWaveTables *out);
 int oz_wave_prep(const OzWaveTables &t, cudaStream_t st);
 int oz_wave_reassemble(const OzWaveTables &t, cudaStream_t st);
 
@@ -121,6 +126,7 @@ struct alignas(64) OzGroupProb {
   uint8_t *res;
   int64_t plane;
   int tile_begin, tile_count;
+  int tile_offset;  // first of the problem's own tiles this launch covers
 };
 // Fills the descriptor of one residue GEMM (tile_begin left to the caller).
 int oz_group_prob(const OzGemmLaunch &L, OzGroupProb *out, const char **why);

@@ -209,7 +209,7 @@ __global__ void __launch_bounds__(NUM_THREADS, 1)
           tmap_acquire(&P.tmB);
           cur = pi;
         }
-        const Tile T = decode(P, t - P.tile_begin);
+        const Tile T = decode(P, t - P.tile_begin + P.tile_offset);
         const int ya = (int)((T.l - P.l0) * P.Mp + (int64_t)T.ti * BM);
         const int yb = (int)((T.l - P.l0) * P.Np + (int64_t)T.tj * BN);
         for (int ks = T.ks0; ks < T.ks1; ++ks) {
@@ -238,7 +238,7 @@ __global__ void __launch_bounds__(NUM_THREADS, 1)
       bool ok = true, any = false;
       for (int t = blockIdx.x; ok && t < p.total_tiles; t += gridDim.x) {
         const OzGroupProb &P = probs[find_problem(probs, p.nprob, t)];
-        const Tile T = decode(P, t - P.tile_begin);
+        const Tile T = decode(P, t - P.tile_begin + P.tile_offset);
         const int nslab = T.ks1 - T.ks0;
         const int nchunk = (nslab + CHUNK_SLABS - 1) / CHUNK_SLABS;
         for (int c = 0; ok && c < nchunk; ++c) {
@@ -288,7 +288,7 @@ __global__ void __launch_bounds__(NUM_THREADS, 1)
     bool ok = true;
     for (int t = blockIdx.x; ok && t < p.total_tiles; t += gridDim.x) {
       const OzGroupProb &P = probs[find_problem(probs, p.nprob, t)];
-      const Tile T = decode(P, t - P.tile_begin);
+      const Tile T = decode(P, t - P.tile_begin + P.tile_offset);
       const int nslab = T.ks1 - T.ks0;
       const int nchunk = (nslab + CHUNK_SLABS - 1) / CHUNK_SLABS;
       const float m = p.mod_f[T.l], inv = p.inv_f[T.l];

@@ -461,6 +461,13 @@ size_t oz_wave_table_bytes(int nitems) {
 }
 
 int oz_wave_tables(const OzWaveItem *items, int n, void *dev, OzWaveTables *out) {
+  std::vector<char> image;
+  oz_wave_image(items, n, dev, image, out);
+  return cudaMemcpy(dev, image.data(), image.size(), cudaMemcpyHostToDevice) == cudaSuccess ? UVATRMM_OK
+                                                                                          : UVATRMM_EDEVICE;
+}
+
+void oz_wave_image(const OzWaveItem *items, int n, void *dev, std::vector<char> &image, OzWaveTables *out) {
   std::vector<ScaleJob> sj(2 * n);
   std::vector<ResidueJob> rj(2 * n);
   std::vector<CrtJob> cj(n);
@@ -504,11 +511,10 @@ int oz_wave_tables(const OzWaveItem *items, int n, void *dev, OzWaveTables *out)
   out->b_scale = bs;
   out->b_resid = br;
   out->b_crt = bc;
-  if (cudaMemcpy(out->scale, sj.data(), sj.size() * sizeof(ScaleJob), cudaMemcpyHostToDevice) != cudaSuccess ||
-      cudaMemcpy(out->resid, rj.data(), rj.size() * sizeof(ResidueJob), cudaMemcpyHostToDevice) != cudaSuccess ||
-      cudaMemcpy(out->crt, cj.data(), cj.size() * sizeof(CrtJob), cudaMemcpyHostToDevice) != cudaSuccess)
-    return UVATRMM_EDEVICE;
-  return UVATRMM_OK;
+  image.assign(oz_wave_table_bytes(n), 0);
+  memcpy(image.data(), sj.data(), sj.size() * sizeof(ScaleJob));
+  memcpy(image.data() + (static_cast<char *>(out->resid) - base), rj.data(), rj.size() * sizeof(ResidueJob));
+  memcpy(image.data() + (static_cast<char *>(out->crt) - base), cj.data(), cj.size() * sizeof(CrtJob));
 }
 
 int oz_wave_prep(const OzWaveTables &t, cudaStream_t st) {

@@ -481,7 +481,7 @@ __global__ void __launch_bounds__(Cfg<BM>::THREADS, Cfg<BM>::MIN_BLOCKS)
         const int pi = find_problem(probs, nprob, t);
         const Fp64GroupProb &P = probs[pi];
         const TileProb tp = P.tp;
-        const int r = t - P.tile_begin;
+        const int r = t - P.tile_begin + P.tile_offset;
         int ti, tj, kt0, kt1;
         decode_major(tp, tp.n_major - 1 - r / tp.n_minor, r % tp.n_minor, ti, tj);
         tile_kslabs(tp, ti, tj, BM, kt0, kt1);

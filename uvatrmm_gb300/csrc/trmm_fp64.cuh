@@ -58,6 +58,7 @@ struct alignas(64) Fp64GroupProb {
   TileProb tp;
   int lk, rk;
   int tile_begin, tile_count;
+  int tile_offset;  // first of the problem's own tiles this launch covers
 };
 
 // Fills `out` for problem L with tile edge BM (tile_begin left to the caller).
