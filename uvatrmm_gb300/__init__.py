@@ -198,7 +198,7 @@ class Server:
         check(lib().uvatrmm_server_submit(self.s, C.byref(pr), int(on_device), C.byref(rid)))
         return rid.value
 
-    def wait(self, rid: int, timeout_s: float = -1.0) -> int:
+    def wait(self, rid: int, timeout_s: float = 300.0) -> int:
         return lib().uvatrmm_server_wait(self.s, rid, timeout_s)
 
     def cancel(self, rid: int) -> int:
