@@ -343,12 +343,31 @@ bool launch_tick(uvatrmm_server_t s, std::vector<Req *> &act) {
   std::vector<Req *> touched;
   double f_budget = s->cfg.tick_fp64_gflop * 1e9, o_budget = s->cfg.tick_ozaki_gflop * 1e9;
   int f_begin = 0, o_begin = 0;
-  for (Req *r : act) {
-    if (r->next >= r->total) continue;
+  // Order: the oldest request of each tier first, with at most a quarter of
+  // the tier's tick (so nothing starves), then shortest remaining work first
+  // (small requests are not stuck behind large ones).
+  std::vector<Req *> order;
+  std::vector<Req *> rest;
+  Req *oldest[2] = {nullptr, nullptr};
+  for (Req *r : act)
+    if (r->next < r->total) {
+      const int k = r->p.tier == UVATRMM_TIER_OZAKI;
+      if (!oldest[k]) oldest[k] = r;
+      else rest.push_back(r);
+    }
+  std::stable_sort(rest.begin(), rest.end(), [](const Req *a, const Req *b) {
+    return (a->total - a->next) * a->tile_cost < (b->total - b->next) * b->tile_cost;
+  });
+  for (Req *r : oldest)
+    if (r) order.push_back(r);
+  order.insert(order.end(), rest.begin(), rest.end());
+  for (Req *r : order) {
     const bool oz = r->p.tier == UVATRMM_TIER_OZAKI;
     double &budget = oz ? o_budget : f_budget;
     if (budget <= 0) continue;
-    int take = (int)std::min<double>(r->total - r->next, std::max(1.0, std::ceil(budget / r->tile_cost)));
+    const double share = r == oldest[oz ? 1 : 0] ? 0.25 * (oz ? s->cfg.tick_ozaki_gflop : s->cfg.tick_fp64_gflop) * 1e9
+                                                 : budget;
+    int take = (int)std::min<double>(r->total - r->next, std::max(1.0, std::ceil(share / r->tile_cost)));
     if ((int)(oz ? odesc.size() : fdesc.size()) >= s->cfg.max_active) continue;
     budget -= take * r->tile_cost;
     if (oz) {
