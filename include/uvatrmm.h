@@ -144,6 +144,57 @@ UVATRMM_API int uvatrmm_dtrmm_device_noalloc(int layout, int side, int uplo, int
                                             int64_t n, double alpha, const double *dA, int64_t lda, double *dB,
                                             int64_t ldb, void *stream);
 
+/* ---------------------------------------------------------------- GEMM and the reference's stage */
+/* Drop-in for cblas_dgemm (LP64): C := alpha*op(A)*op(B) + beta*C on host
+ * buffers, the reference's other local call (UVaTRMM/src/mm_triangular.c:347-360),
+ * on the same FP64 tile engine as the TRMM.  Errors as cblas_dtrmm. */
+UVATRMM_API void cblas_dgemm(CBLAS_LAYOUT layout, CBLAS_TRANSPOSE transa, CBLAS_TRANSPOSE transb, int M, int N,
+                             int K, double alpha, const double *A, int lda, const double *B, int ldb, double beta,
+                             double *C, int ldc);
+/* The same with a status (host buffers / device buffers on the handle's stream). */
+UVATRMM_API int uvatrmm_dgemm(uvatrmm_handle_t handle, int layout, int transa, int transb, int64_t m, int64_t n,
+                              int64_t k, double alpha, const double *A, int64_t lda, const double *B, int64_t ldb,
+                              double beta, double *C, int64_t ldc);
+UVATRMM_API int uvatrmm_dgemm_device(uvatrmm_handle_t handle, int layout, int transa, int transb, int64_t m,
+                                     int64_t n, int64_t k, double alpha, const double *dA, int64_t lda,
+                                     const double *dB, int64_t ldb, double beta, double *dC, int64_t ldc);
+/* One stage of the reference's product loop (UVaTRMM/src/mm_triangular.c:319-410)
+ * for one column slice, on device buffers, all row-major: with the row block
+ * [b, b+h) of the lower-triangular n x n A as the rank receives it (dAblk, h
+ * rows, lda >= b+h), the slice B (n x w, ldb) and C (ldc):
+ *   C[b:b+h, :]    = Ablk[:, 0:b+1] * B[0:b+1, :]                   (the dgemm)
+ *   C[b+1:b+h, :] += tril(Ablk[1:h, b+1:b+h]) * B[b+1:b+h, :]        (dtrmm + add)
+ * B is not modified (the reference saves and restores it around its
+ * in-place dtrmm).  A caller that receives row blocks (e.g. over MPI/NCCL)
+ * feeds them stage by stage. */
+UVATRMM_API int uvatrmm_stage(uvatrmm_handle_t handle, int64_t n, int64_t w, int64_t b, int64_t h,
+                              const double *dAblk, int64_t lda, const double *dB, int64_t ldb, double *dC,
+                              int64_t ldc);
+
+/* ---------------------------------------------------------------- result files and layouts */
+/* The reference's binary result file (print_output_results_generic,
+ * UVaTRMM/src/mm_triangular_common.c:2134-2163): int rows, int cols, int
+ * {row_begin, nrows, col_begin, ncols}, then nrows rows of ncols doubles
+ * (host, row-major block with leading dimension ld). */
+UVATRMM_API int uvatrmm_write_result(const char *path, int rows, int cols, int row_begin, int nrows, int col_begin,
+                                     int ncols, const double *block, int64_t ld);
+/* Reads such a file: header into hdr[6], data into out (capacity doubles). */
+UVATRMM_API int uvatrmm_read_result(const char *path, int hdr[6], double *out, int64_t capacity);
+/* ScaLAPACK's numroc: rows (or columns) of an n-long dimension split in
+ * blocks of nb owned by process iproc of nprocs when the first block sits
+ * on isrcproc (the layout of ScaLAPACK/scalapack_sample_trmm.c:66-121). */
+UVATRMM_API int64_t uvatrmm_numroc(int64_t n, int64_t nb, int iproc, int isrcproc, int nprocs);
+/* 2-D block-cyclic pieces <-> one column-major matrix on the device.
+ * locals[p*npcol + q] is process (p, q)'s column-major local matrix with
+ * leading dimension lld[p*npcol + q] (both host arrays of device pointers /
+ * sizes); blocks are mb x nb, the first block on process (0, 0). */
+UVATRMM_API int uvatrmm_bc_gather(uvatrmm_handle_t handle, int64_t m, int64_t n, int64_t mb, int64_t nb, int nprow,
+                                  int npcol, const double *const *locals, const int64_t *lld, double *dglobal,
+                                  int64_t ldg);
+UVATRMM_API int uvatrmm_bc_scatter(uvatrmm_handle_t handle, int64_t m, int64_t n, int64_t mb, int64_t nb, int nprow,
+                                   int npcol, const double *dglobal, int64_t ldg, double *const *locals,
+                                   const int64_t *lld);
+
 /* ---------------------------------------------------------------- Ozaki (emulated FP64) */
 /* The same TRMM computed exactly in integer arithmetic on the bf16 tensor
  * cores and rounded once to FP64 (Ozaki-style splitting with `moduli`

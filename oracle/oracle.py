@@ -169,6 +169,13 @@ def blas_dtrmm(layout, side, uplo, transa, diag, m, n, alpha, A, lda, B, ldb) ->
     assert rc == 0
 
 
+def blas_dgemm(layout, ta, tb, m, n, k, alpha, A, lda, B, ldb, beta, Cm, ldc) -> None:
+    """OpenBLAS cblas_dgemm (the local GEMM of UVaTRMM/src/mm_triangular.c:347-360), in place on Cm."""
+    blas_ready()
+    rc = lib().orc_blas_dgemm(layout, ta, tb, m, n, k, alpha, _ptr(A), lda, _ptr(B), ldb, beta, _ptr(Cm), ldc)
+    assert rc == 0
+
+
 def uvatrmm_product(n: int, P: int, balanced: bool, A: np.ndarray, B: np.ndarray) -> np.ndarray:
     """UVaTRMM/src/mm_triangular.c:319-403 for all P ranks; row-major n x n."""
     blas_ready()
@@ -200,3 +207,94 @@ def ref_binary(name: str) -> str | None:
     """Path of a program built by oracle/build_ref.sh, or None."""
     p = os.path.join(REF_DIR, name)
     return p if os.path.exists(p) else None
+
+
+# ---------------------------------------------------------------- result files
+
+def result_file_bytes(rows: int, cols: int, row_begin: int, nrows: int, col_begin: int, ncols: int,
+                      block: np.ndarray) -> bytes:
+    """The bytes print_output_results_generic writes
+    (UVaTRMM/src/mm_triangular_common.c:2134-2163): the ints rows, cols,
+    row_begin, nrows, col_begin, ncols in native order, then the nrows x ncols
+    row-major block of doubles.  print_output_results (:2103-2131) is the
+    special case row_begin = 0, nrows = rows."""
+    hdr = np.array([rows, cols, row_begin, nrows, col_begin, ncols], dtype=np.intc)
+    body = np.ascontiguousarray(np.asarray(block, dtype=np.float64).reshape(nrows, ncols))
+    return hdr.tobytes() + body.tobytes()
+
+
+# ---------------------------------------------------------------- ScaLAPACK block-cyclic layout
+
+def numroc(n: int, nb: int, iproc: int, isrcproc: int, nprocs: int) -> int:
+    """ScaLAPACK's NUMROC (TOOLS/numroc.f, ScaLAPACK 2.x; the library is not part
+    of the reference, which calls it at ScaLAPACK/scalapack_sample_trmm.c:66-67
+    and scalapack_sample_gemm.c:60-61): how many of the n rows (or columns),
+    dealt out in blocks of nb round-robin from process isrcproc, process iproc
+    holds.  Restated from the published algorithm."""
+    mydist = (nprocs + iproc - isrcproc) % nprocs
+    nblocks = n // nb
+    r = (nblocks // nprocs) * nb
+    extra = nblocks % nprocs
+    if mydist < extra:
+        r += nb
+    elif mydist == extra:
+        r += n % nb
+    return r
+
+
+def _local_to_global(nloc: int, nb: int, me: int, nprocs: int) -> np.ndarray:
+    """Global index of each local index (ScaLAPACK/scalapack_sample_trmm.c:77-86)."""
+    i = np.arange(nloc)
+    return ((i // nb) * nprocs + me) * nb + i % nb
+
+
+def sample_locals(kind: str, n: int, nb: int, nprow: int, npcol: int) -> dict:
+    """Local column-major blocks (mpA x nqA, ld mpA) of the ScaLAPACK samples, in
+    BLACS rank order iam = myrow*npcol + mycol (row-major grid, layout 'R').
+
+    kind "trmm": ScaLAPACK/scalapack_sample_trmm.c:74-96 -- A[k] = 9*iam + counter
+    on and below the diagonal (0 above), B = 1 on and below, 2 above.
+    kind "gemm": ScaLAPACK/scalapack_sample_gemm.c:64-85 -- A[k] = 9*iam + counter
+    everywhere, B = 2 on the diagonal (0 elsewhere), C = 0."""
+    out = {"A": [], "B": [], "C": []}
+    for iam in range(nprow * npcol):
+        myrow, mycol = iam // npcol, iam % npcol
+        mp, nq = numroc(n, nb, myrow, 0, nprow), numroc(n, nb, mycol, 0, npcol)
+        I = _local_to_global(mp, nb, myrow, nprow)[:, None]
+        J = _local_to_global(nq, nb, mycol, npcol)[None, :]
+        # counter runs over local columns, then local rows (k = i + j*mp)
+        k = (np.arange(mp)[:, None] + np.arange(nq)[None, :] * mp).astype(np.float64)
+        if kind == "trmm":
+            low = I >= J
+            A = np.where(low, 9.0 * iam + np.cumsum(low.T.ravel()).reshape(nq, mp).T - 1.0, 0.0)
+            B = np.where(low, 1.0, 2.0)
+        else:
+            A = 9.0 * iam + k
+            B = np.where(I == J, 2.0, 0.0)
+        out["A"].append(np.asfortranarray(A))
+        out["B"].append(np.asfortranarray(B))
+        out["C"].append(np.zeros((mp, nq), order="F"))
+    return out
+
+
+def bc_to_global(locals_: list, m: int, n: int, mb: int, nb: int, nprow: int, npcol: int) -> np.ndarray:
+    """The global m x n matrix whose block-cyclic pieces are locals_ (ordered p*npcol + q)."""
+    G = np.zeros((m, n))
+    for pq, L in enumerate(locals_):
+        p, q = pq // npcol, pq % npcol
+        I = _local_to_global(L.shape[0], mb, p, nprow)
+        J = _local_to_global(L.shape[1], nb, q, npcol)
+        G[np.ix_(I, J)] = L
+    return G
+
+
+def bc_from_global(G: np.ndarray, mb: int, nb: int, nprow: int, npcol: int) -> list:
+    """Block-cyclic pieces of G, ordered p*npcol + q (inverse of bc_to_global)."""
+    m, n = G.shape
+    out = []
+    for pq in range(nprow * npcol):
+        p, q = pq // npcol, pq % npcol
+        I = _local_to_global(numroc(m, mb, p, 0, nprow), mb, p, nprow)
+        J = _local_to_global(numroc(n, nb, q, 0, npcol), nb, q, npcol)
+        out.append(np.asfortranarray(G[np.ix_(I, J)]))
+    return out

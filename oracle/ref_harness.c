@@ -14,6 +14,10 @@
  *   ref_harness gen <n> <row_begin> <rows> <col_begin> <cols> <triangular>
  *       the block produced by mat_consecutive_values, row-major, %.17g
  *       (UVaTRMM/src/mm_triangular_common.c:1782-1805, built with -DMININUMS=1)
+ *   ref_harness result <rows> <cols> <rb> <nrows> <cb> <ncols> <rank> <procs>
+ *       writes ./tests/outputs/output_golden.<rows>.<procs>.<rank>.dat with the
+ *       reference's print_output_results_generic
+ *       (UVaTRMM/src/mm_triangular_common.c:2134-2163) for a fixed block
  */
 #include <stdio.h>
 #include <stdlib.h>
@@ -43,6 +47,19 @@ int main(int argc, char **argv) {
     free(m);
     return 0;
   }
-  fprintf(stderr, "usage: %s maps <n> <P> <reg|balanced> | gen <n> <rb> <rows> <cb> <cols> <tri>\n", argv[0]);
+  if (argc >= 10 && !strcmp(argv[1], "result")) {
+    /* Block entries are 0.25*k + 1/3 for k = 0, 1, ... in row-major order. */
+    int rows = atoi(argv[2]), cols = atoi(argv[3]);
+    Range lr = {strtoul(argv[4], 0, 10), strtoul(argv[5], 0, 10)};
+    Range lc = {strtoul(argv[6], 0, 10), strtoul(argv[7], 0, 10)};
+    int rank = atoi(argv[8]), procs = atoi(argv[9]);
+    double *m = calloc(lr.size * lc.size + 1, sizeof(double));
+    for (unsigned long i = 0; i < lr.size * lc.size; i++) m[i] = 0.25 * (double)i + 1.0 / 3.0;
+    print_output_results_generic(rows, cols, lr, lc, rank, m, procs, "golden");
+    free(m);
+    return 0;
+  }
+  fprintf(stderr, "usage: %s maps <n> <P> <reg|balanced> | gen <n> <rb> <rows> <cb> <cols> <tri> |"
+          " result <rows> <cols> <rb> <nrows> <cb> <ncols> <rank> <procs>\n", argv[0]);
   return 2;
 }

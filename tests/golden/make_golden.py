@@ -11,6 +11,8 @@ the reference.
   consecutive.json  blocks made by mat_consecutive_values
                     (UVaTRMM/src/mm_triangular_common.c:1782-1805), via ref_harness
   cli_stdout.txt    one full stdout of `uvatrmm.x 64 balanced trapezoid` (format pin)
+  result_files.json bytes of result files written by print_output_results_generic
+                    (UVaTRMM/src/mm_triangular_common.c:2134-2163), via ref_harness
 
 Usage: python tests/golden/make_golden.py   (after oracle/build_ref.sh)
 """
@@ -76,7 +78,22 @@ def main():
     with open(os.path.join(HERE, "consecutive.json"), "w") as f:
         json.dump({"source": "reference mat_consecutive_values (-DMININUMS=1) via oracle/_ref/ref_harness",
                    "blocks": blocks}, f)
-    print("wrote norms.json, mappings.json, consecutive.json, cli_stdout.txt")
+
+    # Result files written by the reference's own print_output_results_generic.
+    results = []
+    with tempfile.TemporaryDirectory() as tmp:
+        os.makedirs(os.path.join(tmp, "tests", "outputs"))
+        for (rows, cols, rb, nr, cb, nc, rank, procs) in [(5, 7, 0, 5, 2, 3, 1, 4), (6, 6, 2, 3, 0, 6, 0, 2),
+                                                           (4, 9, 0, 4, 0, 0, 3, 4), (1, 1, 0, 1, 0, 1, 0, 1)]:
+            run([HARNESS, "result", str(rows), str(cols), str(rb), str(nr), str(cb), str(nc), str(rank),
+                 str(procs)], cwd=tmp)
+            path = os.path.join(tmp, "tests", "outputs", f"output_golden.{rows}.{procs}.{rank}.dat")
+            with open(path, "rb") as f:
+                results.append({"args": [rows, cols, rb, nr, cb, nc, rank, procs], "hex": f.read().hex()})
+    with open(os.path.join(HERE, "result_files.json"), "w") as f:
+        json.dump({"source": "reference print_output_results_generic via oracle/_ref/ref_harness; "
+                   "block entries 0.25*k + 1/3 row-major", "files": results}, f, indent=1)
+    print("wrote norms.json, mappings.json, consecutive.json, cli_stdout.txt, result_files.json")
 
 
 if __name__ == "__main__":

@@ -89,6 +89,31 @@ class Handle:
     def sync(self) -> None:
         check(lib().uvatrmm_sync(self.h))
 
+    # -- GEMM, the product loop's stage, block-cyclic layouts -------------------
+    def dgemm(self, layout, transa, transb, m, n, k, alpha, A, lda, B, ldb, beta, C_, ldc) -> None:
+        """Host buffers (numpy float64): C := alpha*op(A)*op(B) + beta*C."""
+        check(lib().uvatrmm_dgemm(self.h, layout, transa, transb, m, n, k, alpha, _ptr(A), lda, _ptr(B), ldb,
+                                  beta, _ptr(C_), ldc))
+
+    def dgemm_device(self, layout, transa, transb, m, n, k, alpha, dA, lda, dB, ldb, beta, dC, ldc) -> None:
+        check(lib().uvatrmm_dgemm_device(self.h, layout, transa, transb, m, n, k, alpha, _ptr(dA), lda,
+                                         _ptr(dB), ldb, beta, _ptr(dC), ldc))
+
+    def stage(self, n, w, b, h, dAblk, lda, dB, ldb, dC, ldc) -> None:
+        """One step of the row-block product loop (row-major device buffers)."""
+        check(lib().uvatrmm_stage(self.h, n, w, b, h, _ptr(dAblk), lda, _ptr(dB), ldb, _ptr(dC), ldc))
+
+    def bc_gather(self, m, n, mb, nb, nprow, npcol, locals_, llds, dglobal, ldg) -> None:
+        """Block-cyclic local blocks (device, column-major, process (p,q) at p*npcol+q) -> global."""
+        ptrs = (C.c_void_p * len(locals_))(*[_ptr(x) for x in locals_])
+        ld = (C.c_int64 * len(llds))(*llds)
+        check(lib().uvatrmm_bc_gather(self.h, m, n, mb, nb, nprow, npcol, ptrs, ld, _ptr(dglobal), ldg))
+
+    def bc_scatter(self, m, n, mb, nb, nprow, npcol, dglobal, ldg, locals_, llds) -> None:
+        ptrs = (C.c_void_p * len(locals_))(*[_ptr(x) for x in locals_])
+        ld = (C.c_int64 * len(llds))(*llds)
+        check(lib().uvatrmm_bc_scatter(self.h, m, n, mb, nb, nprow, npcol, _ptr(dglobal), ldg, ptrs, ld))
+
     # -- Ozaki (emulated FP64) --------------------------------------------------
     def ozaki_device(self, layout, side, uplo, transa, diag, m, n, alpha, dA, lda, dB, ldb, moduli=0,
                      want_err=False):
@@ -240,3 +265,34 @@ def map_rows(schedule: int, n: int, nblocks: int, idx: int):
     b, s = C.c_uint64(), C.c_uint64()
     rc = lib().uvatrmm_map_rows(schedule, n, nblocks, idx, C.byref(b), C.byref(s))
     return None if rc else (b.value, s.value)
+
+
+def numroc(n: int, nb: int, iproc: int, isrcproc: int, nprocs: int) -> int:
+    """Rows (or columns) of an n-long block-cyclic dimension held by process iproc."""
+    return lib().uvatrmm_numroc(n, nb, iproc, isrcproc, nprocs)
+
+
+def write_result(path: str, rows: int, cols: int, row_begin: int, nrows: int, col_begin: int, ncols: int,
+                 block, ld: int) -> None:
+    """Writes one rank's result block in the reference's binary result-file format."""
+    check(lib().uvatrmm_write_result(path.encode(), rows, cols, row_begin, nrows, col_begin, ncols,
+                                     _ptr(block) if block is not None else None, ld))
+
+
+def read_result(path: str, out=None):
+    """Reads a result file: (header of 6 ints, block as a flat float64 numpy array)."""
+    import numpy as np
+    import sys
+    hdr = (C.c_int * 6)()
+    try:
+        with open(path, "rb") as f:  # sizes the buffer; the library parses and checks the file
+            raw = f.read(24)
+    except OSError as e:
+        raise UvatrmmError(EINVAL, f"cannot open {path}: {e}") from None
+    if len(raw) != 24:
+        raise UvatrmmError(EINVAL, f"malformed result file: {path}")
+    nr = int.from_bytes(raw[12:16], sys.byteorder, signed=True)
+    nc = int.from_bytes(raw[20:24], sys.byteorder, signed=True)
+    buf = np.empty(max(nr, 0) * max(nc, 0), dtype=np.float64) if out is None else out
+    check(lib().uvatrmm_read_result(path.encode(), hdr, buf.ctypes.data if buf.size else None, buf.size))
+    return list(hdr), buf

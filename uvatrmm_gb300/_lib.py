@@ -83,6 +83,15 @@ SIGNATURES.update({
                                   C.POINTER(i32), C.POINTER(i64)]),
     "uvatrmm_group_destroy": (i32, [vp]),
     "uvatrmm_tune": (i32, [vp, i32, i32, i64, i64, C.POINTER(i32)]),
+    "cblas_dgemm": (None, [i32, i32, i32, i32, i32, i32, dbl, vp, i32, vp, i32, dbl, vp, i32]),
+    "uvatrmm_dgemm": (i32, [vp, i32, i32, i32, i64, i64, i64, dbl, vp, i64, vp, i64, dbl, vp, i64]),
+    "uvatrmm_dgemm_device": (i32, [vp, i32, i32, i32, i64, i64, i64, dbl, vp, i64, vp, i64, dbl, vp, i64]),
+    "uvatrmm_stage": (i32, [vp, i64, i64, i64, i64, vp, i64, vp, i64, vp, i64]),
+    "uvatrmm_write_result": (i32, [C.c_char_p, i32, i32, i32, i32, i32, i32, vp, i64]),
+    "uvatrmm_read_result": (i32, [C.c_char_p, C.POINTER(i32), vp, i64]),
+    "uvatrmm_numroc": (i64, [i64, i64, i32, i32, i32]),
+    "uvatrmm_bc_gather": (i32, [vp, i64, i64, i64, i64, i32, i32, C.POINTER(vp), C.POINTER(i64), vp, i64]),
+    "uvatrmm_bc_scatter": (i32, [vp, i64, i64, i64, i64, i32, i32, vp, i64, C.POINTER(vp), C.POINTER(i64)]),
 })
 
 

@@ -127,7 +127,7 @@ bool tma_ok(const void *p, int64_t ld) { return (reinterpret_cast<uintptr_t>(p) 
 // Launches C := alpha*op(A)*B or alpha*B*op(A) on device buffers, all
 // column-major; A and B must satisfy tma_ok.
 int run_fp64(uvatrmm_handle_t h, const Trmm &t, const double *A, int64_t lda, const double *B, int64_t ldb,
-             double *C, int64_t ldc, int schedule, int shape) {
+             double *C, int64_t ldc, int schedule, int shape, double beta = 0.0) {
   Fp64Launch L;
   const int64_t ka = t.side == CblasLeft ? t.m : t.n;
   const bool lower = (t.uplo == CblasLower) != (t.trans != 0);
@@ -135,6 +135,7 @@ int run_fp64(uvatrmm_handle_t h, const Trmm &t, const double *A, int64_t lda, co
   L.N = t.n;
   L.K = ka;
   L.alpha = t.alpha;
+  L.beta = beta;
   L.C = C;
   L.ldc = ldc;
   L.unit = t.unit;
@@ -177,7 +178,7 @@ int zero_device(uvatrmm_handle_t h, double *dB, int64_t ldb, int64_t rows, int64
 // dC receives the result (may equal dB only when `in_place`).
 int device_trmm(uvatrmm_handle_t h, int layout, int side, int uplo, int transa, int diag, int64_t m, int64_t n,
                 double alpha, const double *dA, int64_t lda, const double *dB, int64_t ldb, double *dC,
-                int64_t ldc, bool in_place, int schedule, int shape) {
+                int64_t ldc, bool in_place, int schedule, int shape, double beta) {
   if (int bad = check_args(layout, side, uplo, transa, diag, m, n, lda, ldb))
     return fail(UVATRMM_EINVAL, "parameter " + std::to_string(bad) + " had an illegal value");
   if (!in_place) {
@@ -186,7 +187,10 @@ int device_trmm(uvatrmm_handle_t h, int layout, int side, int uplo, int transa, 
   }
   Trmm t = normalise(layout, side, uplo, transa, diag, m, n, alpha);
   if (t.m == 0 || t.n == 0) return ok();
-  if (alpha == 0.0) return zero_device(h, dC, ldc, t.m, t.n) == UVATRMM_OK ? ok() : tl_status;
+  if (alpha == 0.0) {
+    if (beta == 0.0) return zero_device(h, dC, ldc, t.m, t.n) == UVATRMM_OK ? ok() : tl_status;
+    return scale_device(h, dC, ldc, t.m, t.n, beta) == UVATRMM_OK ? ok() : tl_status;
+  }
   const int64_t ka = t.side == CblasLeft ? t.m : t.n;
   const double *A = dA;
   int64_t la = lda;
@@ -208,7 +212,7 @@ int device_trmm(uvatrmm_handle_t h, int layout, int side, int uplo, int transa, 
     if (e != cudaSuccess) return cuda_fail(e, "staging B");
     B = w;
   }
-  int rc = run_fp64(h, t, A, la, B, lb, dC, ldc, schedule, shape);
+  int rc = run_fp64(h, t, A, la, B, lb, dC, ldc, schedule, shape, beta);
   return rc == UVATRMM_OK ? ok() : rc;
 }
 

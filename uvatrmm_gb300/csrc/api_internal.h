@@ -72,7 +72,7 @@ Trmm normalise(int layout, int side, int uplo, int transa, int diag, int64_t m, 
 // in place, through workspace slots 0 and 1).
 int device_trmm(uvatrmm_handle_t h, int layout, int side, int uplo, int transa, int diag, int64_t m, int64_t n,
                 double alpha, const double *dA, int64_t lda, const double *dB, int64_t ldb, double *dC,
-                int64_t ldc, bool in_place, int schedule, int shape);
+                int64_t ldc, bool in_place, int schedule, int shape, double beta = 0.0);
 
 // Ozaki emulated TRMM on device buffers, in place on dB (ozaki_api.cu).
 int ozaki_device(uvatrmm_handle_t h, int layout, int side, int uplo, int transa, int diag, int64_t m, int64_t n,
@@ -82,6 +82,9 @@ int ozaki_device(uvatrmm_handle_t h, int layout, int side, int uplo, int transa,
 // Autotuner (tune.cu): tuned tile edge (FP64) or raster group (Ozaki) for a
 // problem shape; measures and caches a missing bucket when h->autotune.
 int tune_choice(uvatrmm_handle_t h, int tier, int side, int64_t m, int64_t n, int *choice);
+
+// C := beta * C over a column-major rows x cols device block (extras.cu).
+int scale_device(uvatrmm_handle_t h, double *C, int64_t ldc, int64_t rows, int64_t cols, double beta);
 
 // ||X - R||_F / ||R||_F over column-major device blocks.
 int rel_frobenius(uvatrmm_handle_t h, int64_t rows, int64_t cols, const double *X, int64_t ldx, const double *R,

@@ -103,7 +103,10 @@ __device__ __forceinline__ double tri_select(double v, int cls, int unit) {
 
 __device__ __forceinline__ void tile_kslabs(const TileProb &p, int ti, int tj, int BM, int &kt0, int &kt1) {
   int64_t kb, ke;
-  if (p.tri_left) {
+  if (p.tri_none) {
+    kb = 0;
+    ke = p.K;
+  } else if (p.tri_left) {
     int64_t i0 = (int64_t)ti * BM;
     if (p.tri_lower) { kb = 0; ke = min(i0 + BM, p.K); }
     else { kb = i0; ke = p.K; }
@@ -114,6 +117,12 @@ __device__ __forceinline__ void tile_kslabs(const TileProb &p, int ti, int tj, i
   }
   kt0 = (int)(kb / kBK);
   kt1 = (int)((ke + kBK - 1) / kBK);
+}
+
+// Epilogue store: alpha * acc, plus beta * C when beta != 0 (C unread otherwise).
+__device__ __forceinline__ void out_store(const TileProb &p, int64_t i, int64_t j, double acc) {
+  double *c = p.C + i + j * p.ldc;
+  *c = p.beta != 0.0 ? fma(p.beta, *c, p.alpha * acc) : p.alpha * acc;
 }
 
 __device__ __forceinline__ void decode_major(const TileProb &p, int r, int minor, int &ti, int &tj) {
@@ -202,7 +211,7 @@ struct DfmaEngine {
 #pragma unroll
       for (int ii = 0; ii < C::TM; ++ii) {
         int64_t i = i0 + ty + C::TY * ii;
-        if (i < p.M) p.C[i + j * p.ldc] = p.alpha * acc[ii][jj];
+        if (i < p.M) out_store(p, i, j, acc[ii][jj]);
       }
     }
   }
@@ -294,8 +303,8 @@ struct DmmaEngine {
         int64_t i = i0 + r0 + 8 * f + g;
         int64_t j = j0 + c0 + 8 * h + 2 * t;
         if (i < p.M) {
-          if (j < p.N) p.C[i + j * p.ldc] = p.alpha * acc[f][h][0];
-          if (j + 1 < p.N) p.C[i + (j + 1) * p.ldc] = p.alpha * acc[f][h][1];
+          if (j < p.N) out_store(p, i, j, acc[f][h][0]);
+          if (j + 1 < p.N) out_store(p, i, j + 1, acc[f][h][1]);
         }
       }
   }
@@ -412,7 +421,7 @@ __global__ void __launch_bounds__(Cfg<BM>::THREADS, Cfg<BM>::MIN_BLOCKS)
       const int64_t i0 = (int64_t)inf.ti * BM, j0 = (int64_t)inf.tj * C::BN;
       const int64_t k0 = (int64_t)inf.kt * kBK;
       const int64_t d0 = p.tri_left ? i0 : j0;
-      if (k0 >= d0 && k0 < d0 + BM)
+      if (!p.tri_none && k0 >= d0 && k0 < d0 + BM)
         eng.template slab_diag<LK, RK>(Lst(s), Rst(s), (int)((k0 - d0) / kBK), p);
       else
         eng.template slab<LK, RK>(Lst(s), Rst(s));
@@ -539,7 +548,7 @@ __global__ void __launch_bounds__(Cfg<BM>::THREADS, Cfg<BM>::MIN_BLOCKS)
       const int64_t d0 = tp.tri_left ? i0 : j0;
       const double *Ls = Lst(s), *Rs = Rst(s);
       const int lay = (P.lk ? 2 : 0) | (P.rk ? 1 : 0);
-      if (k0 >= d0 && k0 < d0 + BM) {
+      if (!tp.tri_none && k0 >= d0 && k0 < d0 + BM) {
         const int sd = (int)((k0 - d0) / kBK);
         switch (lay) {
           case 3: eng.template slab_diag<true, true>(Ls, Rs, sd, tp); break;
@@ -637,8 +646,9 @@ int launch_trmm_fp64(const Fp64Launch &L, cudaStream_t stream, const char **why)
   KParams kp;
   memset(&kp, 0, sizeof(kp));
   kp.M = L.M; kp.N = L.N; kp.K = L.K; kp.ldc = L.ldc;
-  kp.alpha = L.alpha; kp.C = L.C; kp.counter = L.counter; kp.status = L.status;
+  kp.alpha = L.alpha; kp.beta = L.beta; kp.C = L.C; kp.counter = L.counter; kp.status = L.status;
   kp.tri_left = L.tri_left; kp.tri_lower = L.tri_lower; kp.unit = L.unit;
+  kp.tri_none = L.tri_none;
   kp.trapezoid = L.shape == UVATRMM_SHAPE_TRAPEZOID;
   const int tiles_m = (int)((L.M + BM - 1) / BM), tiles_n = (int)((L.N + BM - 1) / BM);
   kp.n_major = L.tri_left ? tiles_m : tiles_n;
@@ -706,8 +716,9 @@ int fp64_group_prob(const Fp64Launch &L, int BM, Fp64GroupProb *out, const char 
   }
   TileProb &tp = out->tp;
   tp.M = L.M; tp.N = L.N; tp.K = L.K; tp.ldc = L.ldc;
-  tp.alpha = L.alpha; tp.C = L.C;
+  tp.alpha = L.alpha; tp.beta = L.beta; tp.C = L.C;
   tp.tri_left = L.tri_left; tp.tri_lower = L.tri_lower; tp.unit = L.unit;
+  tp.tri_none = L.tri_none;
   tp.trapezoid = L.shape == UVATRMM_SHAPE_TRAPEZOID;
   const int tiles_m = (int)((L.M + BM - 1) / BM), tiles_n = (int)((L.N + BM - 1) / BM);
   tp.n_major = L.tri_left ? tiles_m : tiles_n;

@@ -37,6 +37,8 @@ struct Fp64Launch {
   int *counter;    // device int, dynamic schedule (zeroed by the launcher)
   int *status;     // device int, kernel error flags (KERR_*)
   int num_sms;
+  double beta = 0.0;     // C = alpha*op*B + beta*C (0: C is only written)
+  bool tri_none = false;  // plain GEMM: neither operand triangular
 };
 
 // Enqueues the kernel on `stream`.  Returns a uvatrmm_status.
@@ -45,9 +47,10 @@ int launch_trmm_fp64(const Fp64Launch &L, cudaStream_t stream, const char **why)
 // What the kernel's tile walk, engines and epilogue need about one problem.
 struct TileProb {
   int64_t M, N, K, ldc;
-  double alpha;
+  double alpha, beta;  // C = alpha * Lft * Rgt + beta * C (C is not read when beta == 0)
   double *C;
   int tri_left, tri_lower, unit, trapezoid;
+  int tri_none;                     // no triangular operand: a plain GEMM over all of K
   int n_major, n_minor, major_rev;  // tiles along the triangular dimension / the other one
 };
 
