@@ -250,6 +250,8 @@ def run_gpu(args, ws, rank, local):
     del hA, hB, hB0
     if not args.no_ozaki:
         out["ozaki"] = run_ozaki(args, h, dev, stream, rank, achieved)
+    if args.next_n > 0:
+        out["next_rows"] = run_next_rows(args, h, dev, stream, peak)
     if args.batch > 0:
         hb = u.Handle(stream=stream)  # its own workspace for the one-call-per-problem comparison
         out["batch"] = run_batch(args, hb, dev, stream)
@@ -417,6 +419,98 @@ def run_batch(args, h, dev, stream):
             "speedup_vs_one_call_per_problem": round(seq_ms / ms, 3)}
 
 
+def _timed(stream, fn, steps):
+    """Mean CUDA-event ms of fn() over `steps` calls on `stream` (after one warm-up call)."""
+    import torch
+    fn()
+    torch.cuda.synchronize()
+    times = []
+    for _ in range(steps):
+        e0, e1 = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
+        e0.record(stream)
+        fn()
+        e1.record(stream)
+        torch.cuda.synchronize()
+        times.append(e0.elapsed_time(e1))
+    return statistics.mean(times)
+
+
+def run_next_rows(args, h, dev, stream, fp64_peak):
+    """The entry points either side of the TRMM: GEMM, the reference's product
+    loop driven stage by stage, and the ScaLAPACK block-cyclic adapters."""
+    import numpy as np
+    import torch
+
+    import uvatrmm_gb300 as u
+    n = args.next_n
+    out = {}
+    dA = torch.empty(n * n, dtype=torch.float64, device=dev)
+    dB = torch.empty_like(dA)
+    dC = torch.empty_like(dA)
+    h.gen_uniform(5, 0, n, n, dA, 1, n)
+    h.gen_uniform(5, 1, n, n, dB, 1, n)
+    h.sync()
+    # DGEMM n^3 (2 n^3 flop)
+    ms = _timed(stream, lambda: h.dgemm_device(u.COL, u.NOTRANS, u.NOTRANS, n, n, n, 1.0, dA, n, dB, n, 0.0, dC, n),
+                args.next_steps)
+    tf = 2.0 * n ** 3 / (ms * 1e-3) / 1e12
+    out["dgemm"] = {"workload": f"uvatrmm_dgemm_device m=n=k={n} NN alpha=1 beta=0", "value": round(tf, 4),
+                    "unit": "TFLOP/s", "ms": round(ms, 3), "frac_of_fp64_issue_limit": round(tf / fp64_peak, 4)}
+    # The reference's product loop (4 balanced row blocks, one rank owning all columns), stage by stage.
+    h.gen_uniform(5, 2, n, n, dA, 1, n, tri="U")  # row-major lower triangle = column-major upper
+    h.sync()
+    torch.cuda.synchronize()
+    P = 4
+    blocks = [u.map_rows(u.SCHED_BALANCED, n, P, s) for s in range(P)]
+
+    def loop():
+        for b, hh in blocks:
+            h.stage(n, n, b, hh, dA[b * n:], n, dB, n, dC, n)
+    ms = _timed(stream, loop, args.next_steps)
+    tf = float(n) ** 3 / (ms * 1e-3) / 1e12
+    # parity: the same product through one plain TRMM call (row-major left lower), sampled columns
+    dR = dB.clone()
+    torch.cuda.synchronize()  # the clone ran on torch's stream, the library runs on `stream`
+    h.dtrmm_device(u.ROW, u.LEFT, u.LOWER, u.NOTRANS, u.NONUNIT, n, n, 1.0, dA, n, dR, n)
+    h.sync()
+    cols = torch.tensor([0, n // 3, n - 1], device=dev)
+    got = dC.view(n, n)[:, cols].cpu().numpy()
+    ref = dR.view(n, n)[:, cols].cpu().numpy()
+    del dR
+    out["stage_loop"] = {"workload": f"uvatrmm_stage x {P} balanced row blocks, n={n}, one rank (all columns)",
+                         "value": round(tf, 4), "unit": "TFLOP/s (n^3)", "ms": round(ms, 3),
+                         "gpu_launches": 2 * P,
+                         "rel_fro_vs_single_trmm_call": float(np.linalg.norm(got - ref) / np.linalg.norm(ref))}
+    # Block-cyclic gather + scatter of one n x n matrix (2x2 grid, 256 x 256 blocks): 2 reads + 2 writes of 8n^2 bytes.
+    nb, pr, pc = 256, 2, 2
+    loc = []
+    lld = []
+    for pq in range(pr * pc):
+        mp, nq = u.numroc(n, nb, pq // pc, 0, pr), u.numroc(n, nb, pq % pc, 0, pc)
+        loc.append(torch.empty(mp * nq, dtype=torch.float64, device=dev))
+        lld.append(max(mp, 1))
+    h.bc_scatter(n, n, nb, nb, pr, pc, dB, n, loc, lld)
+    ms = _timed(stream, lambda: (h.bc_scatter(n, n, nb, nb, pr, pc, dB, n, loc, lld),
+                                 h.bc_gather(n, n, nb, nb, pr, pc, loc, lld, dC, n)), args.next_steps)
+    gbs = 4 * 8 * n * n / (ms * 1e-3) / 1e9
+    hbm, _ = hbm_peak()
+    out["block_cyclic"] = {"workload": f"uvatrmm_bc_scatter + uvatrmm_bc_gather, {n}x{n}, nb={nb}, {pr}x{pc} grid",
+                           "value": round(gbs, 1), "unit": "GB/s", "ms": round(ms, 3),
+                           "frac_of_measured_hbm": round(gbs / hbm, 4),
+                           "round_trip_exact": bool(torch.equal(dB, dC))}
+    del dA, dB, dC, loc
+    torch.cuda.empty_cache()
+    return out
+
+
+def hbm_peak():
+    try:
+        with open(os.path.join(ROOT, "MEASURED_PEAKS.json")) as f:
+            return float(json.load(f)["hbm_gbs"]), "measured (MEASURED_PEAKS.json)"
+    except Exception:
+        return 6800.0, "fallback (profiling recipe)"
+
+
 def bf16_peak():
     """Sustained cuBLAS bf16 TFLOP/s from MEASURED_PEAKS.json (driver-measured), else the fallback."""
     try:
@@ -538,6 +632,8 @@ def main():
     ap.add_argument("--no-ozaki", action="store_true")
     ap.add_argument("--ozaki-n", type=int, default=32768)
     ap.add_argument("--ozaki-steps", type=int, default=3)
+    ap.add_argument("--next-n", type=int, default=8192)
+    ap.add_argument("--next-steps", type=int, default=3)
     ap.add_argument("--batch", type=int, default=2000)
     ap.add_argument("--batch-steps", type=int, default=2)
     ap.add_argument("--serve", type=int, default=300)

@@ -112,17 +112,30 @@ int device_gemm(uvatrmm_handle_t h, int layout, int ta, int tb, int64_t m, int64
   return ok();
 }
 
-__global__ void bc_kernel(int64_t m, int64_t n, int64_t mb, int64_t nb, int nprow, int npcol, double *const *locals,
-                          const int64_t *lld, double *global, int64_t ldg, int to_global) {
-  const int64_t total = m * n;
-  for (int64_t e = blockIdx.x * (int64_t)blockDim.x + threadIdx.x; e < total; e += (int64_t)gridDim.x * blockDim.x) {
-    const int64_t J = e / m, I = e - J * m;
-    const int p = (int)((I / mb) % nprow), q = (int)((J / nb) % npcol);
-    const int64_t li = (I / (mb * nprow)) * mb + I % mb, lj = (J / (nb * npcol)) * nb + J % nb;
-    const int pq = p * npcol + q;
-    double *loc = locals[pq] + li + lj * lld[pq];
-    if (to_global) global[I + J * ldg] = *loc;
-    else *loc = global[I + J * ldg];
+// One mb x nb block of the global matrix per CTA iteration.  Global block
+// (bi, bj) lives on process (bi mod nprow, bj mod npcol) at local block
+// (bi div nprow, bj div npcol); its columns are contiguous runs of mb doubles
+// in both layouts, so a warp moves 256 consecutive bytes per column.
+constexpr int kBcRows = 32, kBcCols = 8;
+
+__global__ void __launch_bounds__(kBcRows *kBcCols)
+    bc_kernel(int64_t m, int64_t n, int64_t mb, int64_t nb, int nprow, int npcol, double *const *locals,
+              const int64_t *lld, double *global, int64_t ldg, int to_global) {
+  const int64_t nbr = (m + mb - 1) / mb, nbc = (n + nb - 1) / nb;
+  for (int64_t blk = blockIdx.x; blk < nbr * nbc; blk += gridDim.x) {
+    const int64_t bi = blk % nbr, bj = blk / nbr;
+    const int pq = (int)(bi % nprow) * npcol + (int)(bj % npcol);
+    const int64_t ld = lld[pq];
+    double *loc = locals[pq] + (bi / nprow) * mb + (bj / npcol) * nb * ld;
+    double *glb = global + bi * mb + bj * nb * ldg;
+    const int64_t rows = min(mb, m - bi * mb), cols = min(nb, n - bj * nb);
+    const double *__restrict__ src = to_global ? loc : glb;
+    double *__restrict__ dst = to_global ? glb : loc;
+    const int64_t lds = to_global ? ld : ldg, ldd = to_global ? ldg : ld;
+    for (int64_t c = threadIdx.y; c < cols; c += kBcCols) {
+#pragma unroll 4
+      for (int64_t r = threadIdx.x; r < rows; r += kBcRows) dst[r + c * ldd] = src[r + c * lds];
+    }
   }
 }
 
@@ -144,8 +157,10 @@ int bc_move(uvatrmm_handle_t h, int64_t m, int64_t n, int64_t mb, int64_t nb, in
   cudaError_t e = cudaMemcpyAsync(dptr, locals, (size_t)np * 8, cudaMemcpyHostToDevice, h->stream);
   if (e == cudaSuccess) e = cudaMemcpyAsync(dlld, lld, (size_t)np * 8, cudaMemcpyHostToDevice, h->stream);
   if (e != cudaSuccess) return cuda_fail(e, "block-cyclic tables");
-  bc_kernel<<<grid_of(h, m * n), 256, 0, h->stream>>>(m, n, mb, nb, nprow, npcol, dptr, dlld, global, ldg,
-                                                      to_global ? 1 : 0);
+  const int64_t blocks = ((m + mb - 1) / mb) * ((n + nb - 1) / nb);
+  const int grid = (int)std::min<int64_t>(blocks, (int64_t)h->num_sms * 8);
+  bc_kernel<<<grid, dim3(kBcRows, kBcCols), 0, h->stream>>>(m, n, mb, nb, nprow, npcol, dptr, dlld, global, ldg,
+                                                            to_global ? 1 : 0);
   e = cudaGetLastError();
   if (e == cudaSuccess) e = cudaStreamSynchronize(h->stream);  // the host tables may go away after return
   return e == cudaSuccess ? ok() : cuda_fail(e, "block-cyclic copy");
