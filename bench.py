@@ -250,6 +250,8 @@ def run_gpu(args, ws, rank, local):
     del hA, hB, hB0
     if not args.no_ozaki:
         out["ozaki"] = run_ozaki(args, h, dev, stream, rank, achieved)
+    if args.variants:
+        out["variants"] = run_variants(args, h, dev, stream, peak)
     if args.next_n > 0:
         out["next_rows"] = run_next_rows(args, h, dev, stream, peak)
     if args.batch > 0:
@@ -419,10 +421,11 @@ def run_batch(args, h, dev, stream):
             "speedup_vs_one_call_per_problem": round(seq_ms / ms, 3)}
 
 
-def _timed(stream, fn, steps):
-    """Mean CUDA-event ms of fn() over `steps` calls on `stream` (after one warm-up call)."""
+def _timed(stream, fn, steps, warm=True):
+    """Mean CUDA-event ms of fn() over `steps` calls on `stream` (after one warm-up call if `warm`)."""
     import torch
-    fn()
+    if warm:
+        fn()
     torch.cuda.synchronize()
     times = []
     for _ in range(steps):
@@ -433,6 +436,72 @@ def _timed(stream, fn, steps):
         torch.cuda.synchronize()
         times.append(e0.elapsed_time(e1))
     return statistics.mean(times)
+
+
+def run_variants(args, h, dev, stream, fp64_peak):
+    """The plain FP64 configuration's other cases: both uplo under every schedule and
+    message shape at m = n = 16384, the skinny m = 16384, n = 256 case, and m = n = 32768."""
+    import torch
+
+    import uvatrmm_gb300 as u
+    hbm, _ = hbm_peak()
+    out = {"cases": []}
+    m = args.n
+    dA = torch.empty(m * m, dtype=torch.float64, device=dev)
+    dB = torch.empty(m * m, dtype=torch.float64, device=dev)
+    dC = torch.empty_like(dB)
+    h.gen_uniform(1, 1, m, m, dB, 1, m)
+    combos = [(u.SCHED_DYNAMIC, u.SHAPE_TRAPEZOID, "dynamic/trapezoid"), (u.SCHED_REG, u.SHAPE_BOXES, "reg/boxes"),
+              (u.SCHED_REG, u.SHAPE_TRAPEZOID, "reg/trapezoid"), (u.SCHED_BALANCED, u.SHAPE_BOXES, "balanced/boxes"),
+              (u.SCHED_BALANCED, u.SHAPE_TRAPEZOID, "balanced/trapezoid")]
+    for uplo, uname in ((u.LOWER, "L"), (u.UPPER, "U")):
+        h.gen_uniform(1, 0, m, m, dA, 1, m, tri=uname)
+        h.sync()
+        for sched, shape, name in combos:
+            h.set_option("schedule", sched)
+            h.set_option("shape", shape)
+            ms = _timed(stream, lambda: h.dtrmm_device_oop(u.COL, u.LEFT, uplo, u.NOTRANS, u.NONUNIT, m, m, 1.0,
+                                                           dA, m, dB, m, dC, m), 1, warm=False)
+            tf = float(m) ** 3 / (ms * 1e-3) / 1e12
+            out["cases"].append({"m": m, "n": m, "uplo": uname, "schedule/shape": name, "tflops": round(tf, 4),
+                                 "frac_of_fp64_issue_limit": round(tf / fp64_peak, 4), "ms": round(ms, 2)})
+    h.set_option("schedule", u.SCHED_DYNAMIC)
+    h.set_option("shape", u.SHAPE_TRAPEZOID)
+    # skinny: B is m x 256; bytes = A triangle + B read + C written
+    ns = 256
+    h.gen_uniform(1, 0, m, m, dA, 1, m, tri="L")
+    h.sync()
+    ms = _timed(stream, lambda: h.dtrmm_device_oop(u.COL, u.LEFT, u.LOWER, u.NOTRANS, u.NONUNIT, m, ns, 1.0,
+                                                   dA, m, dB, m, dC, m), 3)
+    tf = float(m) * m * ns / (ms * 1e-3) / 1e12
+    gbs = 8.0 * (m * (m + 1) / 2 + 2 * m * ns) / (ms * 1e-3) / 1e9
+    out["skinny"] = {"m": m, "n": ns, "tflops": round(tf, 4), "frac_of_fp64_issue_limit": round(tf / fp64_peak, 4),
+                     "algorithmic_gbs": round(gbs, 1), "frac_of_measured_hbm": round(gbs / hbm, 4),
+                     "ms": round(ms, 3),
+                     "note": "arithmetic intensity n/4 = 64 flop/B, far above the FP64 ridge (~0.19 flop/B): "
+                             "still bound by the FP64 pipe"}
+    del dA, dB, dC
+    torch.cuda.empty_cache()
+    if args.big_n > 0:
+        M = args.big_n
+        dA = torch.empty(M * M, dtype=torch.float64, device=dev)
+        dB = torch.empty_like(dA)
+        dC = torch.empty_like(dA)
+        h.gen_uniform(1, 0, M, M, dA, 1, M, tri="L")
+        h.gen_uniform(1, 1, M, M, dB, 1, M)
+        h.sync()
+        e0, e1 = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
+        e0.record(stream)
+        h.dtrmm_device_oop(u.COL, u.LEFT, u.LOWER, u.NOTRANS, u.NONUNIT, M, M, 1.0, dA, M, dB, M, dC, M)
+        e1.record(stream)
+        torch.cuda.synchronize()
+        ms = e0.elapsed_time(e1)
+        tf = float(M) ** 3 / (ms * 1e-3) / 1e12
+        out["large"] = {"m": M, "n": M, "tflops": round(tf, 4), "frac_of_fp64_issue_limit": round(tf / fp64_peak, 4),
+                        "ms": round(ms, 1), "runs": 1, "note": "one timed call after the 16384 runs (warm kernel)"}
+        del dA, dB, dC
+        torch.cuda.empty_cache()
+    return out
 
 
 def run_next_rows(args, h, dev, stream, fp64_peak):
@@ -632,6 +701,8 @@ def main():
     ap.add_argument("--no-ozaki", action="store_true")
     ap.add_argument("--ozaki-n", type=int, default=32768)
     ap.add_argument("--ozaki-steps", type=int, default=3)
+    ap.add_argument("--no-variants", dest="variants", action="store_false")
+    ap.add_argument("--big-n", type=int, default=32768)
     ap.add_argument("--next-n", type=int, default=8192)
     ap.add_argument("--next-steps", type=int, default=3)
     ap.add_argument("--batch", type=int, default=2000)

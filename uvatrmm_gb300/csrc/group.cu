@@ -171,8 +171,8 @@ int build(uvatrmm_group_t g, const uvatrmm_trmm_problem *probs, int count) {
       pl.K = t.side == CblasLeft ? t.m : t.n;
       pl.n_moduli = p.moduli ? p.moduli : ozaki_auto_moduli(pl.K);
       pl.bits = ozaki_bits(pl.n_moduli, pl.K);
-      pl.Mp = round_up(pl.M, 128);
-      pl.Np = round_up(pl.N, 256);
+      pl.Mp = oz_pad_rows(pl.M);
+      pl.Np = oz_pad_cols(pl.N);
       pl.Kp = round_up(pl.K, 64);
       if (int rc = tune_choice(h, UVATRMM_TIER_OZAKI, t.side, t.m, t.n, &it.raster)) return rc;
       ArenaPlan a;

@@ -56,8 +56,13 @@ struct OzPlan {
   int n_moduli;       // N
   int bits;           // t
   int64_t M, N, K;    // canonical GEMM sizes
-  int64_t Mp, Np, Kp; // padded: Mp % 128 == 0, Np % 256 == 0, Kp % 64 == 0
+  int64_t Mp, Np, Kp; // padded: Mp % 256 == 0, Np % 256 == 0, Kp % 64 == 0
 };
+
+// Padded extents of the residue planes: the residue GEMM's CTA pairs cover
+// 256 rows (two 128-row tiles) x 256 columns, its K slabs are 64 wide.
+inline int64_t oz_pad_rows(int64_t M) { return (M + 255) / 256 * 256; }
+inline int64_t oz_pad_cols(int64_t N) { return (N + 255) / 256 * 256; }
 
 // Device pieces (ozaki_prep.cu).
 // Row/column exponents: e[p] = max over valid k of (ilogb|P[p,k]| + 1).

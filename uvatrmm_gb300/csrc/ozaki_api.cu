@@ -51,8 +51,8 @@ int ozaki_device(uvatrmm_handle_t h, int layout, int side, int uplo, int transa,
   plan.K = t.side == CblasLeft ? t.m : t.n;
   plan.n_moduli = moduli ? moduli : ozaki_auto_moduli(plan.K);
   plan.bits = ozaki_bits(plan.n_moduli, plan.K);
-  plan.Mp = round_up(plan.M, 128);
-  plan.Np = round_up(plan.N, 256);
+  plan.Mp = oz_pad_rows(plan.M);
+  plan.Np = oz_pad_cols(plan.N);
   plan.Kp = round_up(plan.K, 64);
   if (bits_out) *bits_out = plan.bits;
 

@@ -1,7 +1,7 @@
 // Exact residue GEMM on the 5th-generation tensor cores (tcgen05, sm_103a).
 //
-// For every modulus m_l and output tile (128 x 256): the K loop runs over
-// 64-wide bf16 slabs staged by TMA (128-byte swizzle, K-major) into a
+// For every modulus m_l and output tile (128 x 256 per CTA): the K loop runs
+// over 64-wide bf16 slabs staged by TMA (128-byte swizzle, K-major) into a
 // 4-stage shared-memory ring; one thread issues tcgen05.mma.kind::f16
 // (bf16 x bf16 -> fp32 in TMEM, M=128 N=256 K=16).  Every 8 slabs (a K chunk
 // of 512) the accumulator is handed to the epilogue warps, which reduce it
@@ -12,10 +12,25 @@
 // integer below 2^24 and fp32 accumulation is exact.  The last two chunks
 // are combined and the tile's residues (0 <= r < m_l) are written as bytes.
 //
+// CTA pairs.  The kernel runs in clusters of two CTAs stacked along M: the
+// pair computes a 256 x 256 block (rows 2*tp*128 + rank*128 for each CTA)
+// over one K range, the union of both row tiles' ranges (the extra slabs of
+// the shorter range only meet zeros of the triangle).  Each CTA loads its own
+// A tile and half of the shared B tile, which TMA multicasts into both CTAs'
+// shared memory, so every B byte leaves L2 once per pair.  A stage is free
+// again when both CTAs' MMAs have read it: each MMA thread's commit arrives
+// on the stage's empty barrier in both CTAs.
+//
+// The accumulators alternate across tiles (chunk g of a CTA uses buffer
+// g & 1).  The second-to-last chunk of a tile is reduced to byte residues in
+// the epilogue's registers and its buffer released at once, so the next
+// tile's first chunk runs while the last chunk is combined and stored.
+//
 // Warp roles (192 threads, one CTA per SM): warp 0 TMA producer, warp 1 TMEM
 // owner + MMA issuer, warps 2-5 epilogue (each bound to its TMEM lane
 // quadrant, warp % 4).  All mbarrier waits are bounded; on expiry the kernel
-// records KERR_WAIT_TIMEOUT, drains its copies and MMAs, frees TMEM and exits.
+// records KERR_WAIT_TIMEOUT, drains its copies and MMAs, frees TMEM and exits
+// (after the pair's closing cluster barrier).
 #include <algorithm>
 #include <cstring>
 
@@ -27,13 +42,18 @@ namespace uvt {
 namespace {
 
 constexpr int BM = 128, BN = 256, BK = 64;
+constexpr int PAIR = 2;          // CTAs per cluster, stacked along M
+constexpr int BH = BN / PAIR;    // rows of the B tile each CTA loads and multicasts
+constexpr uint16_t PAIR_MASK = (1u << PAIR) - 1;
 constexpr int STAGES = 4;
 constexpr int CHUNK_SLABS = 8;  // K chunk of 512 between modular folds
-constexpr uint32_t A_BYTES = BM * BK * 2, B_BYTES = BN * BK * 2;
+constexpr uint32_t A_BYTES = BM * BK * 2, B_BYTES = BN * BK * 2, BH_BYTES = BH * BK * 2;
 constexpr uint32_t STAGE_BYTES = A_BYTES + B_BYTES;
 constexpr int NUM_THREADS = 192;
 constexpr uint32_t TMEM_COLS = 2 * BN;  // two fp32 accumulators of 256 columns
-constexpr size_t SMEM = 1024 + (size_t)STAGES * STAGE_BYTES + 256;
+// Byte residues of a tile's second-to-last chunk, [column word][row] (32 KB).
+constexpr uint32_t R1_BYTES = BM * BN;
+constexpr size_t SMEM = 1024 + (size_t)STAGES * STAGE_BYTES + 256 + R1_BYTES;
 // kind::f16 instruction descriptor: D fp32 (bits 4-5 = 1), A and B bf16
 // (bits 7-9 = 1, 10-12 = 1), both K-major, N/8 at bits 17-22, M/16 at 24-28.
 constexpr uint32_t IDESC = (1u << 4) | (1u << 7) | (1u << 10) | ((uint32_t)(BN >> 3) << 17) | ((uint32_t)(BM >> 4) << 24);
@@ -41,14 +61,14 @@ constexpr uint32_t IDESC = (1u << 4) | (1u << 7) | (1u << 10) | ((uint32_t)(BN >
 // Launch-wide parameters; the problems themselves are OzGroupProb entries in
 // global memory (their tensor maps are read by TMA from there).
 struct GParams {
-  int nprob, total_tiles;
+  int nprob, total_tiles;  // tiles = CTA-pair tiles (256 x 256 per modulus)
   int *status;
   float mod_f[kMaxModuli];
   float inv_f[kMaxModuli];
 };
 
 struct Tile {
-  int l, ti, tj, ks0, ks1;
+  int l, tp, tj, ks0, ks1;  // modulus, pair row tile, column tile, K slab range
 };
 
 __device__ __forceinline__ void tmap_acquire(const CUtensorMap *m) {
@@ -67,25 +87,26 @@ __device__ __forceinline__ int find_problem(const OzGroupProb *probs, int nprob,
   return lo;
 }
 
-// Local tile t of problem p: modulus, tile coordinates and K slab range.
+// Local pair tile t of problem p: modulus, tile coordinates and K slab range.
 __device__ __forceinline__ Tile decode(const OzGroupProb &p, int t) {
   Tile T;
   T.l = p.l0 + t / p.tiles_per_mod;
   int r = t % p.tiles_per_mod;
-  const int n_maj = p.tri_left ? p.tiles_m : p.tiles_n, n_min = p.tri_left ? p.tiles_n : p.tiles_m;
+  const int tpm = p.tiles_m / PAIR;
+  const int n_maj = p.tri_left ? tpm : p.tiles_n, n_min = p.tri_left ? p.tiles_n : tpm;
   // Raster: groups of `group` major tiles in longest-first order; inside a
-  // group the minor index is outer, so concurrent CTAs share both panels.
+  // group the minor index is outer, so concurrent clusters share both panels.
   const int gspan = p.group * n_min;
   const int g = r / gspan, within = r % gspan;
   const int gsize = min(p.group, n_maj - g * p.group);
   const int mi = within / gsize, rank = g * p.group + within % gsize;
   const int ma = p.grows ? (n_maj - 1 - rank) : rank;
-  T.ti = p.tri_left ? ma : mi;
+  T.tp = p.tri_left ? ma : mi;
   T.tj = p.tri_left ? mi : ma;
   int64_t kb, ke;
   if (p.tri_left) {
-    const int64_t i0 = (int64_t)T.ti * BM;
-    if (p.tri_lower) { kb = 0; ke = min(i0 + BM, p.K); }
+    const int64_t i0 = (int64_t)T.tp * (PAIR * BM);
+    if (p.tri_lower) { kb = 0; ke = min(i0 + PAIR * BM, p.K); }
     else { kb = i0; ke = p.K; }
   } else {
     const int64_t j0 = (int64_t)T.tj * BN;
@@ -95,6 +116,37 @@ __device__ __forceinline__ Tile decode(const OzGroupProb &p, int t) {
   T.ks0 = (int)(kb / BK);
   T.ks1 = (int)((ke + BK - 1) / BK);
   return T;
+}
+
+// ---------------------------------------------------------------- cluster helpers
+__device__ __forceinline__ uint32_t cluster_rank() {
+  uint32_t r;
+  asm volatile("mov.u32 %0, %%cluster_ctarank;" : "=r"(r));
+  return r;
+}
+__device__ __forceinline__ uint32_t cluster_index() {
+  uint32_t r;
+  asm volatile("mov.u32 %0, %%clusterid.x;" : "=r"(r));
+  return r;
+}
+__device__ __forceinline__ uint32_t cluster_count() {
+  uint32_t r;
+  asm volatile("mov.u32 %0, %%nclusterid.x;" : "=r"(r));
+  return r;
+}
+__device__ __forceinline__ void cluster_sync() {
+  asm volatile("barrier.cluster.arrive.release.aligned;\n\tbarrier.cluster.wait.acquire.aligned;" ::: "memory");
+}
+
+// 2-D TMA load multicast to the same shared-memory offset (and the same
+// mbarrier offset) in every CTA of `mask`.
+__device__ __forceinline__ void tma_load_2d_mc(void *smem_dst, const CUtensorMap *m, int x, int y, uint64_t *bar,
+                                               uint16_t mask) {
+  asm volatile(
+      "cp.async.bulk.tensor.2d.shared::cluster.global.mbarrier::complete_tx::bytes.multicast::cluster"
+      " [%0], [%1, {%2, %3}], [%4], %5;" ::"r"(smem_u32(smem_dst)),
+      "l"(reinterpret_cast<uint64_t>(m)), "r"(x), "r"(y), "r"(smem_u32(bar)), "h"(mask)
+      : "memory");
 }
 
 // ---------------------------------------------------------------- tcgen05 wrappers
@@ -118,6 +170,15 @@ __device__ __forceinline__ void umma_bf16(uint32_t d_tmem, uint64_t a, uint64_t 
 __device__ __forceinline__ void umma_commit(uint64_t *bar) {
   asm volatile("tcgen05.commit.cta_group::1.mbarrier::arrive::one.shared::cluster.b64 [%0];" ::"r"(smem_u32(bar))
                : "memory");
+}
+
+// Commit whose arrive lands on the barrier at the same offset in every CTA of `mask`.
+__device__ __forceinline__ void umma_commit_mc(uint64_t *bar, uint16_t mask) {
+  asm volatile(
+      "tcgen05.commit.cta_group::1.mbarrier::arrive::one.shared::cluster.multicast::cluster.b64 [%0], %1;" ::"r"(
+          smem_u32(bar)),
+      "h"(mask)
+      : "memory");
 }
 
 __device__ __forceinline__ void tc_fence_before() { asm volatile("tcgen05.fence::before_thread_sync;" ::: "memory"); }
@@ -159,7 +220,7 @@ __device__ __forceinline__ float mod_pos(float v, float m, float inv) {
 }
 
 // ---------------------------------------------------------------- kernel
-__global__ void __launch_bounds__(NUM_THREADS, 1)
+__global__ void __cluster_dims__(PAIR, 1, 1) __launch_bounds__(NUM_THREADS, 1)
     oz_gemm_kernel(const OzGroupProb *__restrict__ probs, const __grid_constant__ GParams p) {
   extern __shared__ uint8_t smem_raw[];
   uint8_t *base = reinterpret_cast<uint8_t *>((reinterpret_cast<uintptr_t>(smem_raw) + 1023) & ~uintptr_t(1023));
@@ -167,14 +228,16 @@ __global__ void __launch_bounds__(NUM_THREADS, 1)
   uint64_t *full = bars, *empty = bars + STAGES;
   uint64_t *cdone = bars + 2 * STAGES, *afree = cdone + 2, *drain = afree + 2;
   uint32_t *tmem_slot = reinterpret_cast<uint32_t *>(drain + 1);
+  uint32_t *r1s = reinterpret_cast<uint32_t *>(base + STAGES * STAGE_BYTES + 256);
   auto smA = [&](int s) { return base + s * STAGE_BYTES; };
   auto smB = [&](int s) { return base + s * STAGE_BYTES + A_BYTES; };
 
   const int warp = threadIdx.x >> 5, lane = threadIdx.x & 31;
+  const uint32_t rank = cluster_rank();
   if (threadIdx.x == 0) {
     for (int s = 0; s < STAGES; ++s) {
       mbar_init(&full[s], 1);
-      mbar_init(&empty[s], 1);
+      mbar_init(&empty[s], PAIR);  // one commit from each CTA's MMA thread
     }
     for (int b = 0; b < 2; ++b) {
       mbar_init(&cdone[b], 1);
@@ -190,7 +253,9 @@ __global__ void __launch_bounds__(NUM_THREADS, 1)
     asm volatile("tcgen05.relinquish_alloc_permit.cta_group::1.sync.aligned;" ::: "memory");
     tc_fence_before();
   }
-  __syncthreads();
+  // Both CTAs' barriers are initialised before either CTA's copies or
+  // commits can reach them.
+  cluster_sync();
   tc_fence_after();
   const uint32_t tmem_base = *reinterpret_cast<volatile uint32_t *>(tmem_slot);
 
@@ -201,7 +266,7 @@ __global__ void __launch_bounds__(NUM_THREADS, 1)
       uint32_t ph = 0, issued = 0, last_ph[STAGES] = {0, 0, 0, 0};
       bool ok = true;
       int cur = -1;
-      for (int t = blockIdx.x; ok && t < p.total_tiles; t += gridDim.x) {
+      for (int t = (int)cluster_index(); ok && t < p.total_tiles; t += (int)cluster_count()) {
         const int pi = find_problem(probs, p.nprob, t);
         const OzGroupProb &P = probs[pi];
         if (pi != cur) {
@@ -210,17 +275,18 @@ __global__ void __launch_bounds__(NUM_THREADS, 1)
           cur = pi;
         }
         const Tile T = decode(P, t - P.tile_begin + P.tile_offset);
-        const int ya = (int)((T.l - P.l0) * P.Mp + (int64_t)T.ti * BM);
-        const int yb = (int)((T.l - P.l0) * P.Np + (int64_t)T.tj * BN);
+        const int ya = (int)((T.l - P.l0) * P.Mp + ((int64_t)T.tp * PAIR + rank) * BM);
+        const int yb = (int)((T.l - P.l0) * P.Np + (int64_t)T.tj * BN + rank * BH);
         for (int ks = T.ks0; ks < T.ks1; ++ks) {
           if (!mbar_wait_bounded(&empty[s], ph ^ 1)) {
             record_error(p.status, KERR_WAIT_TIMEOUT);
             ok = false;
             break;
           }
+          // This CTA's A tile, its half of B for both CTAs, the peer's half of B: STAGE_BYTES.
           mbar_arrive_expect_tx(&full[s], STAGE_BYTES);
           tma_load_2d(smA(s), &P.tmA, ks * BK, ya, &full[s]);
-          tma_load_2d(smB(s), &P.tmB, ks * BK, yb, &full[s]);
+          tma_load_2d_mc(smB(s) + rank * BH_BYTES, &P.tmB, ks * BK, yb, &full[s], PAIR_MASK);
           issued |= 1u << s;
           last_ph[s] = ph;
           if (++s == STAGES) { s = 0; ph ^= 1; }
@@ -234,22 +300,22 @@ __global__ void __launch_bounds__(NUM_THREADS, 1)
     // ------------------------------------------------------------ MMA issuer
     if (lane == 0) {
       int s = 0;
-      uint32_t ph = 0, uses[2] = {0, 0};
+      uint32_t ph = 0, gc = 0;
       bool ok = true, any = false;
-      for (int t = blockIdx.x; ok && t < p.total_tiles; t += gridDim.x) {
+      for (int t = (int)cluster_index(); ok && t < p.total_tiles; t += (int)cluster_count()) {
         const OzGroupProb &P = probs[find_problem(probs, p.nprob, t)];
         const Tile T = decode(P, t - P.tile_begin + P.tile_offset);
         const int nslab = T.ks1 - T.ks0;
         const int nchunk = (nslab + CHUNK_SLABS - 1) / CHUNK_SLABS;
-        for (int c = 0; ok && c < nchunk; ++c) {
-          const int b = c & 1;
-          if (!mbar_wait_bounded(&afree[b], (uses[b] & 1u) ^ 1u)) {
+        for (int c = 0; ok && c < nchunk; ++c, ++gc) {
+          const uint32_t b = gc & 1u, u = gc >> 1;
+          if (!mbar_wait_bounded(&afree[b], (u & 1u) ^ 1u)) {
             record_error(p.status, KERR_WAIT_TIMEOUT);
             ok = false;
             break;
           }
           tc_fence_after();
-          const uint32_t d_tmem = tmem_base + (uint32_t)(b * BN);
+          const uint32_t d_tmem = tmem_base + b * (uint32_t)BN;
           const int sl0 = c * CHUNK_SLABS, sl1 = min(nslab, sl0 + CHUNK_SLABS);
           for (int sl = sl0; sl < sl1; ++sl) {
             if (!mbar_wait_bounded(&full[s], ph)) {
@@ -264,13 +330,12 @@ __global__ void __launch_bounds__(NUM_THREADS, 1)
               const uint32_t acc = (c >= 2 || sl > sl0 || kk > 0) ? 1u : 0u;
               umma_bf16(d_tmem, sw128_desc(a0 + kk * 32), sw128_desc(b0 + kk * 32), acc);
             }
-            umma_commit(&empty[s]);
+            umma_commit_mc(&empty[s], PAIR_MASK);  // frees stage s in both CTAs once read
             any = true;
             if (++s == STAGES) { s = 0; ph ^= 1; }
           }
           if (!ok) break;
           umma_commit(&cdone[b]);
-          ++uses[b];
         }
       }
       // Drain: all MMAs this thread issued complete before TMEM is freed.
@@ -284,82 +349,96 @@ __global__ void __launch_bounds__(NUM_THREADS, 1)
     const int quad = warp & 3;
     const int row = quad * 32 + lane;
     const uint32_t lane_base = tmem_base + ((uint32_t)(quad * 32) << 16);
-    uint32_t uses[2] = {0, 0};
+    uint32_t gc = 0;
     bool ok = true;
-    for (int t = blockIdx.x; ok && t < p.total_tiles; t += gridDim.x) {
+    for (int t = (int)cluster_index(); ok && t < p.total_tiles; t += (int)cluster_count()) {
       const OzGroupProb &P = probs[find_problem(probs, p.nprob, t)];
       const Tile T = decode(P, t - P.tile_begin + P.tile_offset);
       const int nslab = T.ks1 - T.ks0;
       const int nchunk = (nslab + CHUNK_SLABS - 1) / CHUNK_SLABS;
       const float m = p.mod_f[T.l], inv = p.inv_f[T.l];
-      for (int c = 0; c < nchunk; ++c) {
-        const int b = c & 1;
-        if (!mbar_wait_bounded(&cdone[b], uses[b] & 1u)) {
+      uint32_t *r1 = r1s + row;  // this row's words of r1s, stride BM (each thread touches only its own)
+      for (int c = 0; c < nchunk; ++c, ++gc) {
+        const uint32_t b = gc & 1u, u = gc >> 1;
+        if (!mbar_wait_bounded(&cdone[b], u & 1u)) {
           record_error(p.status, KERR_WAIT_TIMEOUT);
           ok = false;
           break;
         }
-        ++uses[b];
         tc_fence_after();
-        if (c < nchunk - 2) {
+        const uint32_t tb = lane_base + b * (uint32_t)BN;
+        if (c + 2 < nchunk) {
           // Fold: acc := acc - m * rint(acc / m), exact in fp32.
 #pragma unroll 1
           for (int cb = 0; cb < BN / 32; ++cb) {
             uint32_t v[32];
-            const uint32_t ta = lane_base + (uint32_t)(b * BN + cb * 32);
-            tmem_ld32(ta, v);
+            tmem_ld32(tb + (uint32_t)(cb * 32), v);
             tmem_wait_ld();
 #pragma unroll
             for (int e = 0; e < 32; ++e) {
               const float x = __uint_as_float(v[e]);
               v[e] = __float_as_uint(fmaf(-rintf(x * inv), m, x));
             }
-            tmem_st32(ta, v);
+            tmem_st32(tb + (uint32_t)(cb * 32), v);
           }
           tmem_wait_st();
-          tc_fence_before();
-          __syncwarp();
-          if (lane == 0) mbar_arrive(&afree[b]);
-        } else if (c == nchunk - 1) {
-          // Final: residue of (acc[b] + acc[other]) as bytes.
+        } else if (c + 2 == nchunk) {
+          // Second-to-last chunk: its residues move to shared memory, the buffer is freed now.
+#pragma unroll 1
+          for (int cb = 0; cb < BN / 32; ++cb) {
+            uint32_t v[32];
+            tmem_ld32(tb + (uint32_t)(cb * 32), v);
+            tmem_wait_ld();
+#pragma unroll
+            for (int q = 0; q < 8; ++q) {
+              uint32_t w = 0;
+#pragma unroll
+              for (int e = 0; e < 4; ++e)
+                w |= (uint32_t)(int)mod_pos(__uint_as_float(v[q * 4 + e]), m, inv) << (8 * e);
+              r1[(cb * 8 + q) * BM] = w;
+            }
+          }
+        } else {
+          // Last chunk: residue of (this chunk + the second-to-last) as bytes.
           const bool two = nchunk >= 2;
-          const int64_t i = (int64_t)T.ti * BM + row;
+          const int64_t i = ((int64_t)T.tp * PAIR + rank) * BM + row;
           uint8_t *out = P.res + (int64_t)T.l * P.plane + i;
 #pragma unroll 1
           for (int cb = 0; cb < BN / 32; ++cb) {
-            uint32_t v[32], w[32];
-            tmem_ld32(lane_base + (uint32_t)(b * BN + cb * 32), v);
-            if (two) tmem_ld32(lane_base + (uint32_t)((b ^ 1) * BN + cb * 32), w);
+            uint32_t v[32];
+            tmem_ld32(tb + (uint32_t)(cb * 32), v);
             tmem_wait_ld();
             const int64_t j0 = (int64_t)T.tj * BN + cb * 32;
 #pragma unroll
-            for (int e = 0; e < 32; ++e) {
-              float r = mod_pos(__uint_as_float(v[e]), m, inv);
-              if (two) {
-                r += mod_pos(__uint_as_float(w[e]), m, inv);
+            for (int q = 0; q < 8; ++q) {
+              const uint32_t w = two ? r1[(cb * 8 + q) * BM] : 0u;
+#pragma unroll
+              for (int e = 0; e < 4; ++e) {
+                float r = mod_pos(__uint_as_float(v[q * 4 + e]), m, inv) + (float)((w >> (8 * e)) & 255u);
                 if (r >= m) r -= m;
+                out[(j0 + q * 4 + e) * P.Mp] = (uint8_t)(int)r;
               }
-              out[(j0 + e) * P.Mp] = (uint8_t)(int)r;
             }
           }
-          tc_fence_before();
-          __syncwarp();
-          if (lane == 0) {
-            mbar_arrive(&afree[b]);
-            if (two) mbar_arrive(&afree[b ^ 1]);
-          }
         }
-        // c == nchunk - 2: kept for the final combine, released there.
+        tc_fence_before();
+        __syncwarp();
+        if (lane == 0) mbar_arrive(&afree[b]);
       }
     }
   }
   __syncthreads();
+  // Neither CTA leaves while the other may still multicast into its shared
+  // memory or arrive on its barriers.
+  cluster_sync();
   if (warp == 1) {
     tc_fence_after();
     asm volatile("tcgen05.dealloc.cta_group::1.sync.aligned.b32 %0, %1;" ::"r"(tmem_base), "r"(TMEM_COLS)
                  : "memory");
   }
 }
+
+int g_max_clusters = 0;  // co-resident CTA pairs of oz_gemm_kernel (set by oz_gemm_prepare)
 
 }  // namespace
 
@@ -370,7 +449,7 @@ int oz_group_prob(const OzGemmLaunch &L, OzGroupProb *out, const char **why) {
     *why = "empty residue GEMM";
     return UVATRMM_EINVAL;
   }
-  if (L.Mp % BM || L.Np % BN || L.Kp % BK) {
+  if (L.Mp % (PAIR * BM) || L.Np % BN || L.Kp % BK) {
     *why = "residue planes are not padded to the tile sizes";
     return UVATRMM_EINVAL;
   }
@@ -381,7 +460,7 @@ int oz_group_prob(const OzGemmLaunch &L, OzGroupProb *out, const char **why) {
   }
   if (make_tmap_2d(&out->tmA, CU_TENSOR_MAP_DATA_TYPE_BFLOAT16, 2, L.LR, L.Kp, nmod * L.Mp, L.Kp * 2, BK, BM,
                    true) ||
-      make_tmap_2d(&out->tmB, CU_TENSOR_MAP_DATA_TYPE_BFLOAT16, 2, L.RR, L.Kp, nmod * L.Np, L.Kp * 2, BK, BN,
+      make_tmap_2d(&out->tmB, CU_TENSOR_MAP_DATA_TYPE_BFLOAT16, 2, L.RR, L.Kp, nmod * L.Np, L.Kp * 2, BK, BH,
                    true)) {
     *why = "tensor map encoding failed for the residue planes";
     return UVATRMM_EDEVICE;
@@ -393,7 +472,7 @@ int oz_group_prob(const OzGemmLaunch &L, OzGroupProb *out, const char **why) {
   out->grows = L.tri_left ? L.tri_lower : !L.tri_lower;
   out->tiles_m = (int)(L.Mp / BM);
   out->tiles_n = (int)(L.Np / BN);
-  out->tiles_per_mod = out->tiles_m * out->tiles_n;
+  out->tiles_per_mod = (out->tiles_m / PAIR) * out->tiles_n;
   out->tile_count = out->tiles_per_mod * nmod;
   out->group = L.raster_group > 0 ? L.raster_group : 8;
   out->res = L.res;
@@ -402,11 +481,25 @@ int oz_group_prob(const OzGemmLaunch &L, OzGroupProb *out, const char **why) {
 }
 
 int oz_gemm_prepare() {
-  static bool attr = false;
-  if (!attr) {
+  static bool done = false;
+  if (!done) {
     if (cudaFuncSetAttribute(oz_gemm_kernel, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)SMEM) != cudaSuccess)
       return UVATRMM_EDEVICE;
-    attr = true;
+    int dev = 0, sms = 0;
+    cudaGetDevice(&dev);
+    cudaDeviceGetAttribute(&sms, cudaDevAttrMultiProcessorCount, dev);
+    cudaLaunchConfig_t cfg;
+    memset(&cfg, 0, sizeof(cfg));
+    cfg.gridDim = dim3((unsigned)(sms / PAIR * PAIR), 1, 1);
+    cfg.blockDim = dim3(NUM_THREADS, 1, 1);
+    cfg.dynamicSmemBytes = SMEM;
+    int n = 0;
+    if (cudaOccupancyMaxActiveClusters(&n, oz_gemm_kernel, &cfg) != cudaSuccess || n <= 0) {
+      cudaGetLastError();
+      n = sms / PAIR;
+    }
+    g_max_clusters = n;
+    done = true;
   }
   return UVATRMM_OK;
 }
@@ -428,8 +521,8 @@ int launch_oz_gemm_group(const OzGroupProb *dprobs, int nprob, int total_tiles, 
     *why = "cannot reserve shared memory for the residue GEMM";
     return UVATRMM_EDEVICE;
   }
-  const int grid = std::min(num_sms, total_tiles);
-  oz_gemm_kernel<<<grid, NUM_THREADS, SMEM, st>>>(dprobs, g);
+  const int clusters = std::min(std::min(g_max_clusters, num_sms / PAIR), total_tiles);
+  oz_gemm_kernel<<<std::max(clusters, 1) * PAIR, NUM_THREADS, SMEM, st>>>(dprobs, g);
   cudaError_t e = cudaGetLastError();
   if (e != cudaSuccess) {
     *why = cudaGetErrorString(e);

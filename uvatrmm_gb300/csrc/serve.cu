@@ -638,8 +638,8 @@ UVATRMM_API int uvatrmm_server_submit(uvatrmm_server_t s, const uvatrmm_trmm_pro
     pl.K = t.side == CblasLeft ? t.m : t.n;
     pl.n_moduli = p->moduli ? p->moduli : ozaki_auto_moduli(pl.K);
     pl.bits = ozaki_bits(pl.n_moduli, pl.K);
-    pl.Mp = round_up(pl.M, 128);
-    pl.Np = round_up(pl.N, 256);
+    pl.Mp = oz_pad_rows(pl.M);
+    pl.Np = oz_pad_cols(pl.N);
     pl.Kp = round_up(pl.K, 64);
   }
   if (t.m == 0 || t.n == 0 || t.alpha == 0.0) {

@@ -30,6 +30,9 @@
 //   KERR_WAIT_TIMEOUT, drains its own copies in flight and returns.
 #include <algorithm>
 #include <cmath>
+#include <map>
+#include <mutex>
+#include <tuple>
 #include <vector>
 
 #include "common.cuh"
@@ -610,6 +613,53 @@ int fill_bounds(int schedule, int n, int P, int *bounds) {
   return bounds[P] == n ? 0 : -1;
 }
 
+// Block counts of the static schedules: the (Q, CP) with Q*CP <= slots that
+// minimises the largest CTA's work, where major tile of work rank r costs
+// r + 1 slabs-units (the triangle) and a CTA's work is its row block's cost
+// times its panel's width.  The reference mapping decides where the blocks
+// split; only their number is chosen here.  Results are cached per shape.
+void static_grid(int schedule, int n_major, int n_minor, int slots, int *Q_out, int *CP_out) {
+  static std::mutex mu;
+  static std::map<std::tuple<int, int, int, int>, std::pair<int, int>> cache;
+  const auto key = std::make_tuple(schedule, n_major, n_minor, slots);
+  {
+    std::lock_guard<std::mutex> g(mu);
+    auto it = cache.find(key);
+    if (it != cache.end()) {
+      *Q_out = it->second.first;
+      *CP_out = it->second.second;
+      return;
+    }
+  }
+  std::vector<int> qb(kMaxBlocks + 1), cb(kMaxBlocks + 1);
+  int bestQ = 1, bestCP = 1;
+  double best = -1.0;
+  for (int CP = 1; CP <= std::min(n_minor, kMaxBlocks) && CP <= slots; CP *= 2) {
+    if (fill_bounds(UVATRMM_SCHED_REG, n_minor, CP, cb.data()) != 0) continue;
+    int wmax = 0;
+    for (int c = 0; c < CP; ++c) wmax = std::max(wmax, cb[c + 1] - cb[c]);
+    for (int Q = 1; Q <= std::min(std::min(slots / CP, n_major), kMaxBlocks); ++Q) {
+      if (fill_bounds(schedule, n_major, Q, qb.data()) != 0) continue;
+      double rmax = 0.0;
+      for (int q = 0; q < Q; ++q) {
+        // sum of (r + 1) over ranks r in [qb[q], qb[q+1])
+        const double a = qb[q], b = qb[q + 1];
+        rmax = std::max(rmax, 0.5 * (b * (b + 1) - a * (a + 1)));
+      }
+      const double span = rmax * wmax;
+      if (best < 0 || span < best * (1.0 - 1e-9)) {
+        best = span;
+        bestQ = Q;
+        bestCP = CP;
+      }
+    }
+  }
+  std::lock_guard<std::mutex> g(mu);
+  cache[key] = {bestQ, bestCP};
+  *Q_out = bestQ;
+  *CP_out = bestCP;
+}
+
 }  // namespace
 
 int fp64_auto_tile(int64_t M, int64_t N, int64_t K, int num_sms) {
@@ -666,15 +716,8 @@ int launch_trmm_fp64(const Fp64Launch &L, cudaStream_t stream, const char **why)
     // Q row blocks (reference mapping over the major tiles) x CP column
     // panels (map_regular over the minor tiles), Q*CP <= CTAs resident.
     const int slots = L.num_sms * per_sm;
-    int CP = 1;
-    while (CP * 2 <= kp.n_minor && slots / (CP * 2) >= 2 && kp.n_minor % (CP * 2) == 0 &&
-           slots / (CP * 2) >= kp.n_major / 8)
-      CP *= 2;
-    int Q = std::min(std::min(slots / CP, kp.n_major), kMaxBlocks);
-    CP = std::min(CP, kMaxBlocks);
-    // Shrink Q until the reference mapping accepts it (it aborts when a
-    // block would be empty).
-    while (Q > 1 && fill_bounds(L.schedule, kp.n_major, Q, kp.qb) != 0) --Q;
+    int Q = 1, CP = 1;
+    static_grid(L.schedule, kp.n_major, kp.n_minor, slots, &Q, &CP);
     if (fill_bounds(L.schedule, kp.n_major, Q, kp.qb) != 0 ||
         fill_bounds(UVATRMM_SCHED_REG, kp.n_minor, CP, kp.cb) != 0) {
       *why = "row mapping rejected the tile counts";
