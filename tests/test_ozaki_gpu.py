@@ -88,6 +88,27 @@ def test_ozaki_passes_do_not_change_the_result(handle):
     assert np.array_equal(one, many)
 
 
+@pytest.mark.parametrize("moduli", [2, 3, 5, 8, 12, 16, 20])
+def test_ozaki_exact_forced_slice_counts(handle, moduli):
+    """Integer operands that fit the slice count's bits give the exact product
+    for every slice count: the 64-bit slicing path (bits <= 63), the wide
+    path (20 slices: more than 63 bits), and the CRT reconstruction from one
+    to six 32-bit limbs."""
+    K = 1100 if moduli >= 5 else 64
+    _, bits = u.ozaki_plan(K, moduli)
+    hi = 2 ** min(bits - 1, 11) - 1
+    rng = np.random.default_rng(moduli)
+    m, n = K, 29
+    Af = rng.integers(-hi, hi + 1, size=(K, K)).astype(np.float64)
+    Bf = rng.integers(-hi, hi + 1, size=(m, n)).astype(np.float64)
+    exact = np.tril(Af).astype(np.int64) @ Bf.astype(np.int64)
+    A = np.asfortranarray(Af).ravel(order="F").copy()
+    B = np.asfortranarray(Bf).ravel(order="F").copy()
+    _, got_bits = handle.ozaki(COL, LEFT, LOWER, NOTRANS, NONUNIT, m, n, 1.0, A, K, B, m, moduli=moduli)
+    assert got_bits == bits
+    assert np.array_equal(B.reshape(n, m).T, exact.astype(np.float64))
+
+
 def test_ozaki_wide_exponent_sweep(handle):
     """Entries uniform[-1,1) * 2^k, k in [-20, 20] (the precision config's
     distribution): error falls with the slice count and meets 1e-14 with the

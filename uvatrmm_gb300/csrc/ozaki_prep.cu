@@ -116,6 +116,42 @@ __device__ __forceinline__ void store_residues(const uint32_t (&w)[4], bool neg,
   }
 }
 
+// Integers below 2^63 (every automatic slice count): with 16-bit digits
+// x = d3 2^48 + d2 2^32 + d1 2^16 + d0, x mod m is the residue of
+// d0 + d1 (2^16 mod m) + d2 (2^32 mod m) + d3 (2^48 mod m) < 2^26.
+template <int L>
+__device__ __forceinline__ uint32_t residue64(uint64_t x) {
+  constexpr uint32_t m = (uint32_t)kModuli[L];
+  constexpr uint32_t c16 = pow2mod(16, m), c32 = pow2mod(32, m), c48 = pow2mod(48, m);
+  const uint32_t s = (uint32_t)(x & 0xFFFFu) + (uint32_t)((x >> 16) & 0xFFFFu) * c16 +
+                     (uint32_t)((x >> 32) & 0xFFFFu) * c32 + (uint32_t)(x >> 48) * c48;
+  return s % m;
+}
+
+// bf16 bits of the balanced residue r in (-m/2, m/2] (|value| <= 128: exact).
+template <int L>
+__device__ __forceinline__ uint32_t balanced_bits(uint32_t r) {
+  constexpr int m = kModuli[L];
+  const int rs = (int)r > m / 2 ? (int)r - m : (int)r;
+  return __float_as_uint((float)rs) >> 16;
+}
+
+// Residues of four consecutive-k entries for moduli [l0, l1), one 8-byte
+// store per plane; sg holds each entry's sign bit at bit 15 of its half.
+template <int L>
+__device__ __forceinline__ void store4_residues(const uint64_t (&x)[4], const uint32_t (&sg)[2], int l0, int l1,
+                                                uint16_t *out, int64_t plane) {
+  if constexpr (L < kMaxModuli) {
+    if (L >= l0 && L < l1) {
+      uint2 v;
+      v.x = (balanced_bits<L>(residue64<L>(x[0])) | (balanced_bits<L>(residue64<L>(x[1])) << 16)) ^ sg[0];
+      v.y = (balanced_bits<L>(residue64<L>(x[2])) | (balanced_bits<L>(residue64<L>(x[3])) << 16)) ^ sg[1];
+      *reinterpret_cast<uint2 *>(out + (int64_t)(L - l0) * plane) = v;
+    }
+    store4_residues<L + 1>(x, sg, l0, l1, out, plane);
+  }
+}
+
 // The 32 (p) x 64 (k) residue tile (bx = k tile, by = p tile).
 __device__ __forceinline__ void residue_body(const OzOperand &op, const int *e, int bits, int l0, int l1, int64_t Pp,
                                              int64_t Kp, uint16_t *R, int64_t bx, int64_t by) {
@@ -131,6 +167,32 @@ __device__ __forceinline__ void residue_body(const OzOperand &op, const int *e, 
   }
   __syncthreads();
   const int64_t plane = Pp * Kp;
+  if (bits <= 63) {
+    // Each thread: four consecutive k of rows tid/16 and tid/16 + 16.
+#pragma unroll
+    for (int half = 0; half < 2; ++half) {
+      const int pp = (tid >> 4) + half * (TP / 2), kk0 = (tid & 15) * 4;
+      const int ep = e[p0 + pp];
+      uint64_t x[4];
+      uint32_t sg[2] = {0, 0};
+#pragma unroll
+      for (int q = 0; q < 4; ++q) {
+        const double v = tile[pp][kk0 + q];
+        x[q] = 0;
+        if (v != 0.0 && ep != kExpNone) {
+          const uint64_t b = (uint64_t)__double_as_longlong(v);
+          const int be = (int)((b >> 52) & 0x7FF);
+          const uint64_t mant = be ? ((b & ((1ull << 52) - 1)) | (1ull << 52)) : (b & ((1ull << 52) - 1));
+          const int s = (be ? be - 1075 : -1074) + bits - ep;  // scaled integer = mant * 2^s < 2^bits
+          if (s >= 0) x[q] = mant << s;
+          else if (s > -64) x[q] = (mant + (1ull << (-s - 1))) >> (-s);
+          if (b >> 63) sg[q >> 1] |= 0x8000u << (16 * (q & 1));
+        }
+      }
+      store4_residues<0>(x, sg, l0, l1, R + (p0 + pp) * Kp + (k0 + kk0), plane);
+    }
+    return;
+  }
   for (int idx = tid; idx < TP * TK; idx += 256) {
     const int kk = idx % TK, pp = idx / TK;
     const double v = tile[pp][kk];
@@ -162,105 +224,155 @@ __global__ void __launch_bounds__(256) residue_kernel(OzOperand op, const int *e
 }
 
 // ---------------------------------------------------------------- reassembly
+// 32-bit limbs, least significant first.  S = sum_l r_l W_l < 20 * 2^8 * M
+// needs 6 limbs for 20 moduli (M < 2^157).
+constexpr int kLimbs = 6;
+
 struct CrtConst {
   int n;
   int bits;
-  uint64_t W[kMaxModuli][3];  // W_l = (M/m_l) * ((M/m_l)^-1 mod m_l)
-  uint64_t Mw[3], halfM[3];
-  float Mf;                   // M / 2^128
+  int base;                        // quotient estimate reads limbs base .. base+2
+  float inv_mf;                    // 2^(32 base) / M
+  uint32_t W[kMaxModuli][kLimbs];  // W_l = (M/m_l) * ((M/m_l)^-1 mod m_l)
+  uint32_t Mw[kLimbs], halfM[kLimbs];
 };
 
-__device__ __forceinline__ bool ge3(const uint64_t a[3], const uint64_t b[3]) {
-  if (a[2] != b[2]) return a[2] > b[2];
-  if (a[1] != b[1]) return a[1] > b[1];
-  return a[0] >= b[0];
+__device__ __forceinline__ bool lt6(const uint32_t (&a)[kLimbs], const uint32_t (&b)[kLimbs]) {
+#pragma unroll
+  for (int k = kLimbs - 1; k >= 0; --k)
+    if (a[k] != b[k]) return a[k] < b[k];
+  return false;
 }
-__device__ __forceinline__ void sub3(uint64_t a[3], const uint64_t b[3]) {
-  unsigned __int128 t = (unsigned __int128)a[0] - b[0];
-  a[0] = (uint64_t)t;
-  uint64_t br = (uint64_t)(t >> 64) ? 1 : 0;
-  t = (unsigned __int128)a[1] - b[1] - br;
-  a[1] = (uint64_t)t;
-  br = (uint64_t)(t >> 64) ? 1 : 0;
-  a[2] = a[2] - b[2] - br;
+__device__ __forceinline__ void sub6(uint32_t (&a)[kLimbs], const uint32_t (&b)[kLimbs]) {
+  uint32_t br = 0;
+#pragma unroll
+  for (int k = 0; k < kLimbs; ++k) {
+    const uint64_t t = (uint64_t)a[k] - b[k] - br;
+    a[k] = (uint32_t)t;
+    br = (uint32_t)(t >> 63);
+  }
 }
-__device__ __forceinline__ void add3(uint64_t a[3], const uint64_t b[3]) {
-  unsigned __int128 t = (unsigned __int128)a[0] + b[0];
-  a[0] = (uint64_t)t;
-  t = (unsigned __int128)a[1] + b[1] + (uint64_t)(t >> 64);
-  a[1] = (uint64_t)t;
-  a[2] = a[2] + b[2] + (uint64_t)(t >> 64);
+__device__ __forceinline__ void add6(uint32_t (&a)[kLimbs], const uint32_t (&b)[kLimbs]) {
+  uint64_t c = 0;
+#pragma unroll
+  for (int k = 0; k < kLimbs; ++k) {
+    c += (uint64_t)a[k] + b[k];
+    a[k] = (uint32_t)c;
+    c >>= 32;
+  }
 }
 
-// Rows [256 bx, 256 bx + 256) of columns j0, j0 + jstep, ... of C.
+// d * 2^k, exact when the result is a normal double.
+__device__ __forceinline__ double times_pow2(double d, int k) {
+  if (k >= -1022 && k <= 1023) return d * __longlong_as_double((long long)(k + 1023) << 52);
+  return ldexp(d, k);
+}
+
+// One element: residues r_l (byte `sh` of rw[l]) -> C value (alpha applied).
+__device__ __forceinline__ double crt_element(const CrtConst &cc, const uint32_t (&rw)[kMaxModuli], int sh, int er,
+                                              int ec, double alpha) {
+  // S = sum_l r_l W_l: per-limb 64-bit sums (each < 20 * 2^40), carries once.
+  uint64_t acc[kLimbs];
+#pragma unroll
+  for (int k = 0; k < kLimbs; ++k) acc[k] = 0;
+#pragma unroll
+  for (int l = 0; l < kMaxModuli; ++l) {
+    if (l < cc.n) {
+      const uint32_t r = (rw[l] >> sh) & 255u;
+#pragma unroll
+      for (int k = 0; k < kLimbs; ++k) acc[k] += (uint64_t)r * cc.W[l][k];
+    }
+  }
+  uint32_t S[kLimbs];
+  uint64_t c = 0;
+#pragma unroll
+  for (int k = 0; k < kLimbs; ++k) {
+    c += acc[k];
+    S[k] = (uint32_t)c;
+    c >>= 32;
+  }
+  // R = S mod M: fp32 quotient estimate (off by at most one), then one
+  // correction each way.
+  float sf = 0.f;
+#pragma unroll
+  for (int k = kLimbs - 1; k >= 0; --k)
+    if (k >= cc.base && k <= cc.base + 2) sf = fmaf(sf, 4294967296.0f, (float)S[k]);
+  const uint32_t q = (uint32_t)floorf(sf * cc.inv_mf);
+  uint32_t qM[kLimbs];
+  {
+    uint64_t t = 0;
+#pragma unroll
+    for (int k = 0; k < kLimbs; ++k) {
+      t += (uint64_t)q * cc.Mw[k];
+      qM[k] = (uint32_t)t;
+      t >>= 32;
+    }
+  }
+  if (lt6(S, qM)) add6(S, cc.Mw);  // estimate one too high
+  sub6(S, qM);
+  if (!lt6(S, cc.Mw)) sub6(S, cc.Mw);  // estimate one too low
+  // Signed value in (-M/2, M/2].
+  const bool neg = lt6(cc.halfM, S);
+  if (neg) {
+    uint32_t t[kLimbs];
+#pragma unroll
+    for (int k = 0; k < kLimbs; ++k) t[k] = cc.Mw[k];
+    sub6(t, S);
+#pragma unroll
+    for (int k = 0; k < kLimbs; ++k) S[k] = t[k];
+  }
+  // Round the magnitude to FP64 once: a 64-bit window below the top bit,
+  // with a sticky bit for everything under it.
+  int t = 0;
+#pragma unroll
+  for (int k = 1; k < kLimbs; ++k)
+    if (S[k]) t = k;
+  uint64_t top;
+  int ex;
+  if (t == 0) {
+    top = S[0];
+    ex = 0;
+  } else {
+    const int lz = __clz(S[t]);
+    const uint64_t w = ((uint64_t)S[t] << 32) | S[t - 1];
+    const uint32_t below = t >= 2 ? S[t - 2] : 0u;
+    top = lz ? (w << lz) | (below >> (32 - lz)) : w;
+    bool sticky = (lz ? (below << lz) : below) != 0u;
+#pragma unroll
+    for (int k = 0; k < kLimbs - 3; ++k)
+      if (k < t - 2 && S[k]) sticky = true;
+    if (t < 2) sticky = false;
+    top |= sticky ? 1ull : 0ull;
+    ex = 32 * (t - 1) - lz;
+  }
+  const double d = times_pow2(__ull2double_rn(top), ex + er + ec - 2 * cc.bits);
+  return alpha * (neg ? -d : d);
+}
+
+// Rows [1024 bx, 1024 bx + 1024) of columns j0, j0 + jstep, ... of C; each
+// thread takes four consecutive rows (one 4-byte load per residue plane).
 __device__ __forceinline__ void reassemble_body(const CrtConst &cc, const uint8_t *res, int64_t Mp, int64_t plane,
                                                 int64_t M, int64_t N, const int *e_row, const int *e_col,
                                                 double alpha, double *C, int64_t ldc, int64_t bx, int64_t j0,
                                                 int64_t jstep) {
-  const int64_t i = bx * blockDim.x + threadIdx.x;
-  if (i >= M) return;
-  const int er = e_row[i];
+  const int64_t i0 = (bx * blockDim.x + threadIdx.x) * 4;
+  if (i0 >= M) return;
+  const int4 er4 = *reinterpret_cast<const int4 *>(e_row + i0);
+  const int er[4] = {er4.x, er4.y, er4.z, er4.w};
   for (int64_t j = j0; j < N; j += jstep) {
-  const int ec = e_col[j];
-  if (er == kExpNone || ec == kExpNone) {
-    C[i + j * ldc] = alpha * 0.0;
-    continue;
-  }
-  // S = sum_l r_l W_l  (< 2^146: three 64-bit words)
-  uint64_t S[3] = {0, 0, 0};
-  const uint8_t *rp = res + j * Mp + i;
-  for (int l = 0; l < cc.n; ++l) {
-    const uint64_t r = rp[(int64_t)l * plane];
-    unsigned __int128 t = (unsigned __int128)r * cc.W[l][0] + S[0];
-    S[0] = (uint64_t)t;
-    t = (unsigned __int128)r * cc.W[l][1] + S[1] + (uint64_t)(t >> 64);
-    S[1] = (uint64_t)t;
-    S[2] = S[2] + r * cc.W[l][2] + (uint64_t)(t >> 64);
-  }
-  // R = S mod M via an fp32 quotient estimate and one correction each way.
-  const float sf = (float)S[2] + (float)S[1] * 5.42101086e-20f;  // S / 2^128
-  uint32_t q = (uint32_t)floorf(sf / cc.Mf);
-  uint64_t qM[3];
-  {
-    unsigned __int128 t = (unsigned __int128)q * cc.Mw[0];
-    qM[0] = (uint64_t)t;
-    t = (unsigned __int128)q * cc.Mw[1] + (uint64_t)(t >> 64);
-    qM[1] = (uint64_t)t;
-    qM[2] = q * cc.Mw[2] + (uint64_t)(t >> 64);
-  }
-  if (!ge3(S, qM)) add3(S, cc.Mw);  // estimate one too high
-  sub3(S, qM);
-  if (ge3(S, cc.Mw)) sub3(S, cc.Mw);  // estimate one too low
-  // Signed value in (-M/2, M/2].
-  bool neg = false;
-  if (ge3(S, cc.halfM) && !(S[0] == cc.halfM[0] && S[1] == cc.halfM[1] && S[2] == cc.halfM[2])) {
-    uint64_t t[3] = {cc.Mw[0], cc.Mw[1], cc.Mw[2]};
-    sub3(t, S);
-    S[0] = t[0]; S[1] = t[1]; S[2] = t[2];
-    neg = true;
-  }
-  // Round the magnitude to FP64 once: top 64 bits with a sticky bit.
-  uint64_t top;
-  int shift;
-  if (S[2]) {
-    const int lz = __clzll((long long)S[2]);
-    top = lz ? (S[2] << lz) | (S[1] >> (64 - lz)) : S[2];
-    const bool sticky = (lz ? (S[1] << lz) : S[1]) != 0 || S[0] != 0;
-    top |= sticky ? 1ull : 0ull;
-    shift = 128 - lz;
-  } else if (S[1]) {
-    const int lz = __clzll((long long)S[1]);
-    top = lz ? (S[1] << lz) | (S[0] >> (64 - lz)) : S[1];
-    const bool sticky = (lz ? (S[0] << lz) : 0ull) != 0;
-    top |= sticky ? 1ull : 0ull;
-    shift = 64 - lz;
-  } else {
-    top = S[0];
-    shift = 0;
-  }
-  double d = __ull2double_rn(top);
-  d = ldexp(d, shift + er + ec - 2 * cc.bits);
-  C[i + j * ldc] = alpha * (neg ? -d : d);
+    const int ec = e_col[j];
+    uint32_t rw[kMaxModuli];
+    const uint8_t *rp = res + j * Mp + i0;
+#pragma unroll
+    for (int l = 0; l < kMaxModuli; ++l) rw[l] = l < cc.n ? *reinterpret_cast<const uint32_t *>(rp + l * plane) : 0u;
+#pragma unroll
+    for (int q = 0; q < 4; ++q) {
+      if (i0 + q >= M) break;
+      double v;
+      if (er[q] == kExpNone || ec == kExpNone) v = alpha * 0.0;
+      else v = crt_element(cc, rw, 8 * q, er[q], ec, alpha);
+      C[i0 + q + j * ldc] = v;
+    }
   }
 }
 
@@ -441,15 +553,20 @@ CrtConst make_crt(const OzPlan &plan) {
     big_div_small(Ml, (uint64_t)kModuli[l], &mlm);
     const int64_t inv = inv_mod((int64_t)mlm, kModuli[l]);
     const Big W = big_mul_small(Ml, (uint64_t)inv);
-    for (int k = 0; k < 3; ++k) cc.W[l][k] = W.w[k];
+    for (int k = 0; k < kLimbs; ++k) cc.W[l][k] = (uint32_t)(W.w[k / 2] >> (32 * (k % 2)));
   }
   uint64_t r2;
   const Big half = big_div_small(M, 2, &r2);
-  for (int k = 0; k < 3; ++k) {
-    cc.Mw[k] = M.w[k];
-    cc.halfM[k] = half.w[k];
+  int mt = 0;
+  for (int k = 0; k < kLimbs; ++k) {
+    cc.Mw[k] = (uint32_t)(M.w[k / 2] >> (32 * (k % 2)));
+    cc.halfM[k] = (uint32_t)(half.w[k / 2] >> (32 * (k % 2)));
+    if (cc.Mw[k]) mt = k;
   }
-  cc.Mf = (float)((double)M.w[2] + (double)M.w[1] * 0x1p-64 + (double)M.w[0] * 0x1p-128);
+  cc.base = std::min(std::max(mt - 1, 0), kLimbs - 3);
+  double mf = 0.0;  // M / 2^(32 base)
+  for (int k = kLimbs - 1; k >= cc.base; --k) mf = mf * 4294967296.0 + (double)cc.Mw[k];
+  cc.inv_mf = (float)(1.0 / mf);
   return cc;
 }
 }  // namespace
@@ -492,7 +609,7 @@ void oz_wave_image(const OzWaveItem *items, int n, void *dev, std::vector<char> 
     c.plane = pl.Mp * pl.Np;
     c.M = pl.M;
     c.N = pl.N;
-    c.gx = (pl.M + 255) / 256;
+    c.gx = (pl.M + 1023) / 1024;
     c.e_row = it.e_row;
     c.e_col = it.e_col;
     c.alpha = it.alpha;
@@ -538,7 +655,7 @@ int oz_reassemble(const OzPlan &plan, const uint8_t *res, const int *e_row, cons
                   double *C, int64_t ldc, cudaStream_t st) {
   const CrtConst cc = make_crt(plan);
   if (plan.M <= 0 || plan.N <= 0) return UVATRMM_OK;
-  dim3 grid((unsigned)((plan.M + 255) / 256), (unsigned)std::min<int64_t>(plan.N, 65535));
+  dim3 grid((unsigned)((plan.M + 1023) / 1024), (unsigned)std::min<int64_t>(plan.N, 65535));
   reassemble_kernel<<<grid, 256, 0, st>>>(cc, res, plan.Mp, plan.Mp * plan.Np, plan.M, plan.N, e_row, e_col,
                                            alpha, C, ldc);
   return cudaGetLastError() == cudaSuccess ? UVATRMM_OK : UVATRMM_EDEVICE;
