@@ -11,8 +11,9 @@ needed between steps.  TFLOP/s counts m^2*n flops.
             handle's stream, max over ranks
   e2e       the same TRMM through the host C ABI (uvatrmm_dtrmm: pinned host A
             and B copied in, B copied back, every step)
-  roofline  FP64 pipe bound: achieved = m^2*n / mean kernel time; peak = FP64
-            peak measured in this run by the library's probe kernels
+  roofline  FP64 pipe bound: achieved = m^2*n / mean kernel time; peak = the
+            FP64 issue limit (2 DFMA per clock per SM) at the SM clock sampled
+            during the timed region
   cpu_baseline  the reference's per-rank decomposition (cblas_dgemm + cblas_dtrmm
             + add per row block, UVaTRMM/src/mm_triangular.c:319-403) restated in
             oracle/ over OpenBLAS, one rank's column slice of the P=4 balanced
@@ -590,16 +591,18 @@ def bf16_peak():
 
 
 def ozaki_mma_flops(m, n, moduli, side_left=True, lower=True):
-    """bf16 MMA flops the residue GEMM issues for one call (tile-exact)."""
-    BM, BN, BK = 128, 256, 64
-    Mp, Np = -(-m // BM) * BM, -(-n // BN) * BN
+    """bf16 MMA flops the residue GEMM issues for one call (tile-exact): CTA pairs
+    cover 256 rows x 256 columns over one K range (for a triangular left operand,
+    the union of both 128-row tiles' ranges)."""
+    BM, BN, BK, PAIR = 128, 256, 64, 2
+    Mp, Np = -(-m // (PAIR * BM)) * PAIR * BM, -(-n // BN) * BN
     K = m if side_left else n
     total = 0
     if side_left:
-        for ti in range(Mp // BM):
-            i0 = ti * BM
-            kb, ke = (0, min(i0 + BM, K)) if lower else (i0, K)
-            total += (Np // BN) * ((ke + BK - 1) // BK - kb // BK) * BK
+        for tp in range(Mp // (PAIR * BM)):
+            i0 = tp * PAIR * BM
+            kb, ke = (0, min(i0 + PAIR * BM, K)) if lower else (i0, K)
+            total += PAIR * (Np // BN) * ((ke + BK - 1) // BK - kb // BK) * BK
     else:
         for tj in range(Np // BN):
             j0 = tj * BN
