@@ -213,10 +213,11 @@ def run_gpu(args, ws, rank, local):
     h.dtrmm(L, u.LEFT, Lo, NT, NU, m, n, 1.0, hA.numpy(), m, hB.numpy(), m)  # warm-up (allocates workspace)
     if ws > 1:
         torch.distributed.barrier()
-    t0 = time.perf_counter()
-    for _ in range(e2e_steps):
-        h.dtrmm(L, u.LEFT, Lo, NT, NU, m, n, 1.0, hA.numpy(), m, hB.numpy(), m)
-    e2e_s = time.perf_counter() - t0
+    with ClockSampler(local) as clk_e2e:
+        t0 = time.perf_counter()
+        for _ in range(e2e_steps):
+            h.dtrmm(L, u.LEFT, Lo, NT, NU, m, n, 1.0, hA.numpy(), m, hB.numpy(), m)
+        e2e_s = time.perf_counter() - t0
     if ws > 1:
         tt = torch.tensor([e2e_s], device=dev)
         torch.distributed.all_reduce(tt, op=torch.distributed.ReduceOp.MAX)
@@ -233,7 +234,7 @@ def run_gpu(args, ws, rank, local):
                    "parallelism": f"replicas{ws}"},
         "e2e": {"value": round(e2e_value, 4), "unit": "TFLOP/s", "h2d_bytes_per_step": 8 * (m * m + m * n),
                 "d2h_bytes_per_step": 8 * m * n, "api": "uvatrmm_dtrmm (host pointers, pinned)",
-                "steps": e2e_steps},
+                "steps": e2e_steps, "clocks": clk_e2e.summary()},
         "roofline": {"bound": "tensor", "achieved": round(achieved, 4), "peak": round(peak, 4), "unit": "TFLOP/s",
                      "frac": round(achieved / peak, 4),
                      "traffic": TRAFFIC_BYTES_PER_FLOP * flops if m == n else None,

@@ -124,6 +124,14 @@ namespace {
 
 bool tma_ok(const void *p, int64_t ld) { return (reinterpret_cast<uintptr_t>(p) % 16 == 0) && (ld % 2 == 0); }
 
+// 2-D copy; one linear copy when both sides are contiguous.
+cudaError_t copy2d(void *dst, size_t dpitch, const void *src, size_t spitch, size_t width, size_t height,
+                   cudaMemcpyKind kind, cudaStream_t st) {
+  if (width == 0 || height == 0) return cudaSuccess;
+  if (dpitch == width && spitch == width) return cudaMemcpyAsync(dst, src, width * height, kind, st);
+  return cudaMemcpy2DAsync(dst, dpitch, src, spitch, width, height, kind, st);
+}
+
 // Launches C := alpha*op(A)*B or alpha*B*op(A) on device buffers, all
 // column-major; A and B must satisfy tma_ok.
 int run_fp64(uvatrmm_handle_t h, const Trmm &t, const double *A, int64_t lda, const double *B, int64_t ldb,
@@ -356,13 +364,12 @@ UVATRMM_API int uvatrmm_dtrmm(uvatrmm_handle_t h, int layout, int side, int uplo
   double *dB = static_cast<double *>(workspace(h, 1, (size_t)lb * t.n * 8));
   double *dC = static_cast<double *>(workspace(h, 2, (size_t)lb * t.n * 8));
   if (!dA || !dB || !dC) return tl_status;
-  cudaError_t e = cudaMemcpy2DAsync(dA, la * 8, A, lda * 8, ka * 8, ka, cudaMemcpyHostToDevice, h->stream);
-  if (e == cudaSuccess)
-    e = cudaMemcpy2DAsync(dB, lb * 8, B, ldb * 8, t.m * 8, t.n, cudaMemcpyHostToDevice, h->stream);
+  cudaError_t e = copy2d(dA, la * 8, A, lda * 8, ka * 8, ka, cudaMemcpyHostToDevice, h->stream);
+  if (e == cudaSuccess) e = copy2d(dB, lb * 8, B, ldb * 8, t.m * 8, t.n, cudaMemcpyHostToDevice, h->stream);
   if (e != cudaSuccess) return cuda_fail(e, "host to device copy");
   int rc = run_fp64(h, t, dA, la, dB, lb, dC, lb, h->schedule, h->shape);
   if (rc != UVATRMM_OK) return rc;
-  e = cudaMemcpy2DAsync(B, ldb * 8, dC, lb * 8, t.m * 8, t.n, cudaMemcpyDeviceToHost, h->stream);
+  e = copy2d(B, ldb * 8, dC, lb * 8, t.m * 8, t.n, cudaMemcpyDeviceToHost, h->stream);
   if (e != cudaSuccess) return cuda_fail(e, "device to host copy");
   rc = collect_status(h);
   return rc == UVATRMM_OK ? ok() : rc;
