@@ -60,7 +60,7 @@ __device__ __forceinline__ void scale_body(const OzOperand &op, int *e, int64_t 
       int b2 = kExpNone;
       for (int64_t k = kb + ln; k < ke; k += 32) {
         const double v = load_elem(op, p0 + pp, k);
-        if (v != 0.0) b2 = max(b2, exp_above(v));
+        if (__double_as_longlong(v) << 1) b2 = max(b2, exp_above(v));
       }
 #pragma unroll
       for (int o = 16; o; o >>= 1) b2 = max(b2, __shfl_xor_sync(0xffffffffu, b2, o));
@@ -71,7 +71,7 @@ __device__ __forceinline__ void scale_body(const OzOperand &op, int *e, int64_t 
     const int pp = tid & 31, ky = tid >> 5;
     for (int64_t k = kb + ky; k < ke; k += 8) {
       const double v = load_elem(op, p0 + pp, k);
-      if (v != 0.0) best = max(best, exp_above(v));
+      if (__double_as_longlong(v) << 1) best = max(best, exp_above(v));
     }
     atomicMax(&red[pp], best);
     myp = pp;
@@ -179,7 +179,7 @@ __device__ __forceinline__ void residue_body(const OzOperand &op, const int *e, 
       for (int q = 0; q < 4; ++q) {
         const double v = tile[pp][kk0 + q];
         x[q] = 0;
-        if (v != 0.0 && ep != kExpNone) {
+        if ((__double_as_longlong(v) << 1) && ep != kExpNone) {
           const uint64_t b = (uint64_t)__double_as_longlong(v);
           const int be = (int)((b >> 52) & 0x7FF);
           const uint64_t mant = be ? ((b & ((1ull << 52) - 1)) | (1ull << 52)) : (b & ((1ull << 52) - 1));
@@ -199,7 +199,7 @@ __device__ __forceinline__ void residue_body(const OzOperand &op, const int *e, 
     uint32_t w[4] = {0, 0, 0, 0};
     bool neg = false;
     const int ep = e[p0 + pp];
-    if (v != 0.0 && ep != kExpNone) {
+    if ((__double_as_longlong(v) << 1) && ep != kExpNone) {
       const uint64_t b = (uint64_t)__double_as_longlong(v);
       neg = (b >> 63) != 0;
       const int be = (int)((b >> 52) & 0x7FF);
@@ -270,7 +270,7 @@ __device__ __forceinline__ double times_pow2(double d, int k) {
 
 // One element: residues r_l (byte `sh` of rw[l]) -> C value (alpha applied).
 __device__ __forceinline__ double crt_element(const CrtConst &cc, const uint32_t (&rw)[kMaxModuli], int sh, int er,
-                                              int ec, double alpha) {
+                                              int ec, double alpha, bool unit_alpha) {
   // S = sum_l r_l W_l: per-limb 64-bit sums (each < 20 * 2^40), carries once.
   uint64_t acc[kLimbs];
 #pragma unroll
@@ -345,8 +345,32 @@ __device__ __forceinline__ double crt_element(const CrtConst &cc, const uint32_t
     top |= sticky ? 1ull : 0ull;
     ex = 32 * (t - 1) - lz;
   }
-  const double d = times_pow2(__ull2double_rn(top), ex + er + ec - 2 * cc.bits);
-  return alpha * (neg ? -d : d);
+  // top * 2^e2 as a double, rounded to nearest even in integer arithmetic
+  // (GB300's FP64 pipe is narrow); results outside the normal range take
+  // the floating-point path.
+  const int e2 = ex + er + ec - 2 * cc.bits;
+  uint64_t bitsd = 0;
+  if (top) {
+    const int lzt = __clzll((long long)top);
+    const uint64_t x = top << lzt;  // leading one at bit 63
+    uint64_t mant = x >> 11;        // the 53 bits FP64 keeps
+    const uint64_t rem = x & 0x7FFu;
+    if (rem > 0x400u || (rem == 0x400u && (mant & 1u))) ++mant;
+    int e = e2 - lzt + 63;  // exponent of the leading bit
+    if (mant >> 53) {
+      mant >>= 1;
+      ++e;
+    }
+    if (e >= -1022 && e <= 1023) {
+      bitsd = ((uint64_t)(e + 1023) << 52) | (mant & ((1ull << 52) - 1));
+    } else {
+      const double d = times_pow2(__ull2double_rn(top), e2);
+      bitsd = (uint64_t)__double_as_longlong(d);
+    }
+  }
+  if (neg) bitsd ^= 1ull << 63;
+  const double d = __longlong_as_double((long long)bitsd);
+  return unit_alpha ? d : alpha * d;
 }
 
 // Rows [1024 bx, 1024 bx + 1024) of columns j0, j0 + jstep, ... of C; each
@@ -357,6 +381,7 @@ __device__ __forceinline__ void reassemble_body(const CrtConst &cc, const uint8_
                                                 int64_t jstep) {
   const int64_t i0 = (bx * blockDim.x + threadIdx.x) * 4;
   if (i0 >= M) return;
+  const bool unit_alpha = alpha == 1.0;
   const int4 er4 = *reinterpret_cast<const int4 *>(e_row + i0);
   const int er[4] = {er4.x, er4.y, er4.z, er4.w};
   for (int64_t j = j0; j < N; j += jstep) {
@@ -370,7 +395,7 @@ __device__ __forceinline__ void reassemble_body(const CrtConst &cc, const uint8_
       if (i0 + q >= M) break;
       double v;
       if (er[q] == kExpNone || ec == kExpNone) v = alpha * 0.0;
-      else v = crt_element(cc, rw, 8 * q, er[q], ec, alpha);
+      else v = crt_element(cc, rw, 8 * q, er[q], ec, alpha, unit_alpha);
       C[i0 + q + j * ldc] = v;
     }
   }
