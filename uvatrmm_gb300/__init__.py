@@ -62,7 +62,7 @@ class Handle:
 
     def set_option(self, name: str, value: int) -> None:
         key = {"engine": OPT_ENGINE, "schedule": OPT_SCHEDULE, "shape": OPT_SHAPE, "tile": OPT_TILE,
-               "ozaki_scratch_mb": 5, "stage_timing": 6}[name]
+               "ozaki_scratch_mb": 5, "stage_timing": 6, "autotune": 7, "ozaki_raster": 8}[name]
         check(lib().uvatrmm_set_option(self.h, key, int(value)))
 
     def stage_times(self):

@@ -305,6 +305,10 @@ UVATRMM_API int uvatrmm_set_option(uvatrmm_handle_t h, int option, int value) {
       if (value < 64) break;
       h->ozaki_scratch_mb = value;
       return ok();
+    case UVATRMM_OPT_OZAKI_RASTER:
+      if (value < 0 || value > 64) break;
+      h->oz_raster = value;
+      return ok();
     case UVATRMM_OPT_AUTOTUNE:
       if (value != 0 && value != 1) break;
       h->autotune = value != 0;
