@@ -644,10 +644,11 @@ def run_ozaki(args, h, dev, stream, rank, plain_tflops):
     for _ in range(max(1, args.warmup - 2)):
         step()
     times, stages = [], []
-    for _ in range(args.ozaki_steps):
-        ms, _, _ = step()
-        times.append(ms)
-        stages.append(h.stage_times())
+    with ClockSampler(dev.index or 0) as clk:
+        for _ in range(args.ozaki_steps):
+            ms, _, _ = step()
+            times.append(ms)
+            stages.append(h.stage_times())
     t_ms = statistics.mean(times)
     tflops = float(m) * m * n / (t_ms * 1e-3) / 1e12
     st = [statistics.mean(s[k] for s in stages) for k in range(4)]
@@ -688,6 +689,7 @@ def run_ozaki(args, h, dev, stream, rank, plain_tflops):
                      "frac": round(gemm_tflops / peak, 4), "peak_source": peak_src,
                      "flops": "bf16 MMA flops issued (tile-exact) / residue-GEMM GPU time"},
         "slice_sweep": sweep,
+        "clocks": clk.summary(),
     }
 
 

@@ -93,7 +93,7 @@ typedef enum {
   UVATRMM_OPT_STAGE_TIMING = 6,     /* 1: time the stages of each Ozaki call (uvatrmm_stage_times) */
   UVATRMM_OPT_AUTOTUNE = 7,         /* 1 (default): measure untuned shape buckets; 0: defaults only */
   UVATRMM_OPT_OZAKI_RASTER = 8      /* Ozaki residue GEMM of single calls: major tiles per raster
-                                       group (0 = default 8, else 1..64) */
+                                       group (0 = default 2, else 1..64) */
 } uvatrmm_option;
 typedef enum { UVATRMM_ENGINE_DFMA = 0, UVATRMM_ENGINE_DMMA = 1 } uvatrmm_engine;
 /* DYNAMIC: persistent CTAs pull tiles in longest-first order.
@@ -302,7 +302,7 @@ UVATRMM_API int uvatrmm_server_destroy(uvatrmm_server_t server);
 
 /* ---------------------------------------------------------------- autotuner */
 /* The tuned choice for a problem shape: FP64 tier -> output tile edge (64 or
- * 128); Ozaki tier -> residue-GEMM raster group (4, 8 or 16).  Shapes are
+ * 128); Ozaki tier -> residue-GEMM raster group (1, 2 or 4).  Shapes are
  * bucketed by (tier, side, ceil(log2 m), ceil(log2 n)); a missing bucket is
  * measured on the device (when UVATRMM_OPT_AUTOTUNE is 1, the default) and
  * cached in the file named by $UVATRMM_TUNE_CACHE (default

@@ -113,7 +113,7 @@ struct OzGemmLaunch {
   int64_t Mp, Np, Kp, M, N, K;
   int l0, l1;
   bool tri_left, tri_lower;
-  int raster_group = 8;          // major tiles per raster group (0 = default)
+  int raster_group = 0;          // major tiles per raster group (0 = default, 2)
   OzGroupProb *desc = nullptr;   // device slot for the descriptor (single launches)
   int *status;
   int num_sms;

@@ -23,7 +23,7 @@
 //
 // The accumulators alternate across tiles (chunk g of a CTA uses buffer
 // g & 1).  The second-to-last chunk of a tile is reduced to byte residues in
-// the epilogue's registers and its buffer released at once, so the next
+// shared memory and its buffer released at once, so the next
 // tile's first chunk runs while the last chunk is combined and stored.
 //
 // Warp roles (192 threads, one CTA per SM): warp 0 TMA producer, warp 1 TMEM
@@ -474,7 +474,7 @@ int oz_group_prob(const OzGemmLaunch &L, OzGroupProb *out, const char **why) {
   out->tiles_n = (int)(L.Np / BN);
   out->tiles_per_mod = (out->tiles_m / PAIR) * out->tiles_n;
   out->tile_count = out->tiles_per_mod * nmod;
-  out->group = L.raster_group > 0 ? L.raster_group : 8;
+  out->group = L.raster_group > 0 ? L.raster_group : 2;
   out->res = L.res;
   out->plane = L.Mp * L.Np;
   return UVATRMM_OK;

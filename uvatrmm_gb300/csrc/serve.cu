@@ -298,7 +298,7 @@ int setup(uvatrmm_server_t s, Req &r) {
     L.l1 = pl.n_moduli;
     L.tri_left = t.side == CblasLeft;
     L.tri_lower = (t.uplo == CblasLower) != (t.trans != 0);
-    L.raster_group = 8;
+    L.raster_group = 0;
     L.status = s->h->dctl + 1;
     L.num_sms = s->h->num_sms;
     const char *why = nullptr;
