@@ -263,7 +263,7 @@ __global__ void __cluster_dims__(PAIR, 1, 1) __launch_bounds__(NUM_THREADS, 1)
     // ------------------------------------------------------------ TMA producer
     if (lane == 0) {
       int s = 0;
-      uint32_t ph = 0, issued = 0, last_ph[STAGES] = {0, 0, 0, 0};
+      uint32_t ph = 0, issued = 0, last_ph[STAGES] = {};
       bool ok = true;
       int cur = -1;
       for (int t = (int)cluster_index(); ok && t < p.total_tiles; t += (int)cluster_count()) {
