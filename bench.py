@@ -51,6 +51,16 @@ def dist_env():
     return ws, rank, local
 
 
+def max_over_ranks(x: float, ws: int, device=None) -> float:
+    """The maximum of x over all ranks of the process group (x itself for one rank)."""
+    if ws <= 1:
+        return x
+    import torch
+    t = torch.tensor([x], dtype=torch.float64, device=device)
+    torch.distributed.all_reduce(t, op=torch.distributed.ReduceOp.MAX)
+    return t.item()
+
+
 class ClockSampler:
     """nvidia-smi samples (200 ms) during the timed region."""
 
@@ -176,10 +186,7 @@ def run_gpu(args, ws, rank, local):
     torch.cuda.synchronize(dev)
     total_ms = t_start.elapsed_time(t_end)
     per_launch = [a.elapsed_time(b) for a, b in ev]
-    if ws > 1:
-        tt = torch.tensor([total_ms], device=dev)
-        torch.distributed.all_reduce(tt, op=torch.distributed.ReduceOp.MAX)
-        total_ms = tt.item()
+    total_ms = max_over_ranks(total_ms, ws, dev)
     flops = float(m) * m * n
     value = ws * flops * args.steps / (total_ms * 1e-3) / 1e12
     achieved = flops / (statistics.mean(per_launch) * 1e-3) / 1e12
@@ -218,10 +225,7 @@ def run_gpu(args, ws, rank, local):
         for _ in range(e2e_steps):
             h.dtrmm(L, u.LEFT, Lo, NT, NU, m, n, 1.0, hA.numpy(), m, hB.numpy(), m)
         e2e_s = time.perf_counter() - t0
-    if ws > 1:
-        tt = torch.tensor([e2e_s], device=dev)
-        torch.distributed.all_reduce(tt, op=torch.distributed.ReduceOp.MAX)
-        e2e_s = tt.item()
+    e2e_s = max_over_ranks(e2e_s, ws, dev)
     e2e_value = ws * flops * e2e_steps / e2e_s / 1e12
 
     out = {
