@@ -111,6 +111,25 @@ class ClockSampler:
 
 # --------------------------------------------------------------------- CPU arm
 
+def cpu_model() -> str:
+    """The host CPU's model name (lscpu, else /proc/cpuinfo), for the baseline's record."""
+    try:
+        out = subprocess.run(["lscpu"], capture_output=True, text=True, timeout=10).stdout
+        for line in out.splitlines():
+            if line.startswith("Model name:"):
+                return line.split(":", 1)[1].strip()
+    except Exception:
+        pass
+    try:
+        with open("/proc/cpuinfo") as f:
+            for line in f:
+                if line.lower().startswith("model name"):
+                    return line.split(":", 1)[1].strip()
+    except Exception:
+        pass
+    return "unknown"
+
+
 def cpu_reference_sample(n: int, steps: int, warmup: int, threads: int):
     """Time the reference's per-rank product (restated in oracle/ over
     OpenBLAS) for rank 0 of `mpirun -np 4 uvatrmm.x n balanced trapezoid`:
@@ -132,7 +151,7 @@ def cpu_reference_sample(n: int, steps: int, warmup: int, threads: int):
             times.append(dt)
     flops = float(n) * n * w
     t = statistics.mean(times)
-    return {"value": flops / t / 1e12, "unit": "TFLOP/s", "cores": threads, "kind": "port",
+    return {"value": flops / t / 1e12, "unit": "TFLOP/s", "cores": threads, "kind": "port", "cpu": cpu_model(),
             "sample": f"rank 0 of 4 (balanced map): C[:, 0:{w}] = tril(A) B[:, 0:{w}], n={n}, "
                       f"per-row-block cblas_dgemm+cblas_dtrmm+add over OpenBLAS, {threads} threads, "
                       f"mean of {len(times)} runs ({t:.2f} s each)"}
