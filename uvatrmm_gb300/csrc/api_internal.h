@@ -20,9 +20,11 @@ struct uvatrmm_handle_st {
   int64_t ozaki_scratch_mb = 49152;  // residue-plane budget per pass (MiB)
   bool autotune = true;
   int oz_raster = 0;  // residue-GEMM raster group of single Ozaki calls (0 = default)
-  // Grow-only device workspace slots: 0-2 plain-path staging, 3 reductions,
-  // 4 Ozaki scales, 5 Ozaki residue planes, 6 Ozaki product residues,
-  // 7 Ozaki error-estimate scratch.
+  // Grow-only device workspace slots: 0-2 plain-path and GEMM staging,
+  // 3 reductions, 4 Ozaki scales, 5 Ozaki residue planes, 6 Ozaki product
+  // residues, 7 Ozaki error-estimate scratch and the block-cyclic pointer
+  // tables.  Calls on a handle are serialised by `mu` and a slot's contents
+  // live only within one call (a slot that grows first drains the stream).
   static constexpr int kSlots = 8;
   void *ws[kSlots] = {};
   size_t ws_cap[kSlots] = {};
