@@ -73,6 +73,25 @@ def test_ozaki_device_in_place_matches_host(handle):
     assert np.array_equal(dB.cpu().numpy(), host)
 
 
+def test_ozaki_raster_group_does_not_change_the_result(handle):
+    """The raster group only reorders the residue GEMM's tiles: bit-identical results."""
+    m, n = 1100, 700
+    for side in (LEFT, RIGHT):
+        A, lda, B, ldb = make_problem(COL, side, LOWER, m, n)
+        want = B.copy()
+        handle.ozaki(COL, side, LOWER, NOTRANS, NONUNIT, m, n, 1.0, A, lda, want, ldb)
+        try:
+            for g in (1, 3, 16):
+                handle.set_option("ozaki_raster", g)
+                got = B.copy()
+                handle.ozaki(COL, side, LOWER, NOTRANS, NONUNIT, m, n, 1.0, A, lda, got, ldb)
+                assert np.array_equal(got, want), g
+        finally:
+            handle.set_option("ozaki_raster", 0)
+    with pytest.raises(u.UvatrmmError):
+        handle.set_option("ozaki_raster", 65)
+
+
 def test_ozaki_passes_do_not_change_the_result(handle):
     m, n = 640, 300
     A, lda, B, ldb = make_problem(COL, RIGHT, LOWER, m, n)
