@@ -116,39 +116,54 @@ __device__ __forceinline__ void store_residues(const uint32_t (&w)[4], bool neg,
   }
 }
 
-// Integers below 2^63 (every automatic slice count): with 16-bit digits
-// x = d3 2^48 + d2 2^32 + d1 2^16 + d0, x mod m is the residue of
-// d0 + d1 (2^16 mod m) + d2 (2^32 mod m) + d3 (2^48 mod m) < 2^26.
-template <int L>
-__device__ __forceinline__ uint32_t residue64(uint64_t x) {
-  constexpr uint32_t m = (uint32_t)kModuli[L];
-  constexpr uint32_t c16 = pow2mod(16, m), c32 = pow2mod(32, m), c48 = pow2mod(48, m);
-  const uint32_t s = (uint32_t)(x & 0xFFFFu) + (uint32_t)((x >> 16) & 0xFFFFu) * c16 +
-                     (uint32_t)((x >> 32) & 0xFFFFu) * c32 + (uint32_t)(x >> 48) * c48;
-  return s % m;
+// Integers below 2^63 (every automatic slice count) go through the FP32
+// pipe: x = sum_i d_i 2^(11 i) with six 11-bit digits, so x is congruent to
+// s = sum_i d_i (2^(11 i) mod m) < 6 * 2^11 * 2^8 < 2^22 modulo m, exact in
+// fp32.  r = s - m * rint(s / m), rounding by the 1.5 * 2^23 constant in one
+// fma, is congruent to x; the quotient's error (below 0.002) can only move a
+// remainder sitting at +-(m-1)/2 to -+(m+1)/2, so |r| <= 128 as the residue
+// GEMM's exactness bound requires.  The balanced representative may differ
+// from the integer path's at that tie, never its class modulo m.
+
+// Digits d_0 .. d_5 of x as exact floats.
+__device__ __forceinline__ void digits11(uint64_t x, float (&d)[6]) {
+  const uint32_t lo = (uint32_t)x, hi = (uint32_t)(x >> 32);
+  const uint32_t v[6] = {lo & 0x7FFu, (lo >> 11) & 0x7FFu, __funnelshift_r(lo, hi, 22) & 0x7FFu,
+                         (hi >> 1) & 0x7FFu, (hi >> 12) & 0x7FFu, hi >> 23};
+#pragma unroll
+  for (int i = 0; i < 6; ++i) d[i] = __int_as_float((int)(0x4B000000u | v[i])) - 8388608.0f;
 }
 
-// bf16 bits of the balanced residue r in (-m/2, m/2] (|value| <= 128: exact).
+// bf16 bits of a residue of the integer with digits d, modulo kModuli[L].
 template <int L>
-__device__ __forceinline__ uint32_t balanced_bits(uint32_t r) {
+__device__ __forceinline__ uint32_t residue_bits(const float (&d)[6]) {
   constexpr int m = kModuli[L];
-  const int rs = (int)r > m / 2 ? (int)r - m : (int)r;
-  return __float_as_uint((float)rs) >> 16;
+  constexpr float mf = (float)m, inv = 1.0f / (float)m;
+  constexpr float c1 = (float)pow2mod(11, m), c2 = (float)pow2mod(22, m), c3 = (float)pow2mod(33, m),
+                  c4 = (float)pow2mod(44, m), c5 = (float)pow2mod(55, m);
+  float s = fmaf(d[1], c1, d[0]);
+  s = fmaf(d[2], c2, s);
+  s = fmaf(d[3], c3, s);
+  s = fmaf(d[4], c4, s);
+  s = fmaf(d[5], c5, s);
+  const float q = fmaf(s, inv, 12582912.0f) - 12582912.0f;
+  const float r = fmaf(-q, mf, s);
+  return __float_as_uint(r) >> 16;  // |r| <= 128: exact in bf16
 }
 
 // Residues of four consecutive-k entries for moduli [l0, l1), one 8-byte
 // store per plane; sg holds each entry's sign bit at bit 15 of its half.
 template <int L>
-__device__ __forceinline__ void store4_residues(const uint64_t (&x)[4], const uint32_t (&sg)[2], int l0, int l1,
+__device__ __forceinline__ void store4_residues(const float (&d)[4][6], const uint32_t (&sg)[2], int l0, int l1,
                                                 uint16_t *out, int64_t plane) {
   if constexpr (L < kMaxModuli) {
     if (L >= l0 && L < l1) {
       uint2 v;
-      v.x = (balanced_bits<L>(residue64<L>(x[0])) | (balanced_bits<L>(residue64<L>(x[1])) << 16)) ^ sg[0];
-      v.y = (balanced_bits<L>(residue64<L>(x[2])) | (balanced_bits<L>(residue64<L>(x[3])) << 16)) ^ sg[1];
+      v.x = (residue_bits<L>(d[0]) | (residue_bits<L>(d[1]) << 16)) ^ sg[0];
+      v.y = (residue_bits<L>(d[2]) | (residue_bits<L>(d[3]) << 16)) ^ sg[1];
       *reinterpret_cast<uint2 *>(out + (int64_t)(L - l0) * plane) = v;
     }
-    store4_residues<L + 1>(x, sg, l0, l1, out, plane);
+    store4_residues<L + 1>(d, sg, l0, l1, out, plane);
   }
 }
 
@@ -189,7 +204,10 @@ __device__ __forceinline__ void residue_body(const OzOperand &op, const int *e, 
           if (b >> 63) sg[q >> 1] |= 0x8000u << (16 * (q & 1));
         }
       }
-      store4_residues<0>(x, sg, l0, l1, R + (p0 + pp) * Kp + (k0 + kk0), plane);
+      float dg[4][6];
+#pragma unroll
+      for (int q = 0; q < 4; ++q) digits11(x[q], dg[q]);
+      store4_residues<0>(dg, sg, l0, l1, R + (p0 + pp) * Kp + (k0 + kk0), plane);
     }
     return;
   }
