@@ -492,6 +492,15 @@ def run_variants(args, h, dev, stream, fp64_peak):
                                  "frac_of_fp64_issue_limit": round(tf / fp64_peak, 4), "ms": round(ms, 2)})
     h.set_option("schedule", u.SCHED_DYNAMIC)
     h.set_option("shape", u.SHAPE_TRAPEZOID)
+    # the FP64 tensor-core engine (DMMA, mma.sync m8n8k4) on the last uplo's operands
+    h.set_option("engine", u.ENGINE_DMMA)
+    ms = _timed(stream, lambda: h.dtrmm_device_oop(u.COL, u.LEFT, u.UPPER, u.NOTRANS, u.NONUNIT, m, m, 1.0,
+                                                   dA, m, dB, m, dC, m), 1)
+    h.set_option("engine", u.ENGINE_DFMA)
+    tf = float(m) ** 3 / (ms * 1e-3) / 1e12
+    out["dmma_engine"] = {"m": m, "n": m, "uplo": "U", "schedule/shape": "dynamic/trapezoid",
+                          "tflops": round(tf, 4), "frac_of_fp64_issue_limit": round(tf / fp64_peak, 4),
+                          "ms": round(ms, 2)}
     # skinny: B is m x 256; bytes = A triangle + B read + C written
     ns = 256
     h.gen_uniform(1, 0, m, m, dA, 1, m, tri="L")
