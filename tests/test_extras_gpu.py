@@ -68,6 +68,25 @@ def test_dgemm_all_variants(handle, layout, ta, tb):
             assert np.array_equal(dC.cpu().numpy(), got), "device and host entry points disagree"
 
 
+@pytest.mark.parametrize("engine,tile", [(u.ENGINE_DMMA, 64), (u.ENGINE_DFMA, 128), (u.ENGINE_DMMA, 128)])
+def test_dgemm_engines_and_tiles(handle, engine, tile):
+    handle.set_option("engine", engine)
+    handle.set_option("tile", tile)
+    try:
+        for (layout, ta, tb) in ((COL, NOTRANS, TRANS), (ROW, TRANS, NOTRANS)):
+            m, n, k = 150, 97, 211
+            A, lda, B, ldb, Cm, ldc = gemm_operands(layout, ta, tb, m, n, k, 1, seed=13)
+            ref = ref_gemm(layout, ta, tb, m, n, k, 0.75, A, lda, B, ldb, -1.0, Cm, ldc)
+            got = Cm.copy()
+            handle.dgemm(layout, ta, tb, m, n, k, 0.75, A, lda, B, ldb, -1.0, got, ldc)
+            mask = Cm == -7.0
+            assert np.array_equal(got[mask], Cm[mask])
+            assert rel_fro(got[~mask], ref[~mask]) <= 8 * k * EPS
+    finally:
+        handle.set_option("engine", u.ENGINE_DFMA)
+        handle.set_option("tile", 0)
+
+
 def test_dgemm_misaligned_device_operands(handle):
     import torch
     m, n, k = 67, 45, 99
