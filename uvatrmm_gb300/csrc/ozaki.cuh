@@ -120,9 +120,9 @@ struct OzGemmLaunch {
 };
 int launch_oz_gemm(const OzGemmLaunch &L, cudaStream_t st, const char **why);
 
-// One residue GEMM of a grouped launch as the device reads it (64-byte
-// aligned; TMA reads the two tensor maps from global memory).
-struct alignas(64) OzGroupProb {
+// One residue GEMM of a grouped launch as the device reads it (128-byte
+// aligned like CUtensorMap; TMA reads the two tensor maps from global memory).
+struct alignas(128) OzGroupProb {
   CUtensorMap tmA, tmB;
   int64_t Mp, Np, M, N, K;
   int l0, l1;

@@ -52,7 +52,6 @@ __device__ __forceinline__ void scale_body(const OzOperand &op, int *e, int64_t 
   const int64_t p0 = bx * TP;
   const int64_t kb = by * k_per_block, ke = min(op.K, kb + k_per_block);
   int best = kExpNone;
-  int myp;
   if (op.kcontig) {
     // warp w handles rows p0 + w, p0 + w + 8, ...; lanes stride over k
     const int w = tid >> 5, ln = tid & 31;
@@ -66,7 +65,6 @@ __device__ __forceinline__ void scale_body(const OzOperand &op, int *e, int64_t 
       for (int o = 16; o; o >>= 1) b2 = max(b2, __shfl_xor_sync(0xffffffffu, b2, o));
       if (ln == 0) atomicMax(&red[pp], b2);
     }
-    myp = -1;
   } else {
     const int pp = tid & 31, ky = tid >> 5;
     for (int64_t k = kb + ky; k < ke; k += 8) {
@@ -74,9 +72,7 @@ __device__ __forceinline__ void scale_body(const OzOperand &op, int *e, int64_t 
       if (__double_as_longlong(v) << 1) best = max(best, exp_above(v));
     }
     atomicMax(&red[pp], best);
-    myp = pp;
   }
-  (void)myp;
   __syncthreads();
   if (tid < TP && p0 + tid < op.P) {
     if (direct) e[p0 + tid] = red[tid];

@@ -85,7 +85,6 @@ class Pool {
       }
     }
   }
-  size_t size() const { return size_; }
   size_t peak() const { return peak_; }
 
  private:

@@ -54,9 +54,9 @@ struct TileProb {
   int n_major, n_minor, major_rev;  // tiles along the triangular dimension / the other one
 };
 
-// One problem of a grouped launch, as the device reads it (64-byte aligned:
-// the tensor maps are read by TMA from global memory).
-struct alignas(64) Fp64GroupProb {
+// One problem of a grouped launch, as the device reads it (128-byte aligned
+// like CUtensorMap: the tensor maps are read by TMA from global memory).
+struct alignas(128) Fp64GroupProb {
   CUtensorMap tmL, tmR;
   TileProb tp;
   int lk, rk;
