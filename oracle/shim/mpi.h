@@ -1,6 +1,6 @@
 /*
  * Single-rank MPI stand-in used ONLY to compile the reference program
- * (UVaTRMM/src/*.c) as a CPU checker.  It is test infrastructure: nothing in
+ * (the C files of UVaTRMM/src) as a CPU checker.  It is test infrastructure: nothing in
  * the product links it.
  *
  * With one rank every point-to-point call in the reference's broadcast relay
