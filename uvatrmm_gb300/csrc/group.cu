@@ -178,7 +178,7 @@ int build(uvatrmm_group_t g, const uvatrmm_trmm_problem *probs, int count) {
       ArenaPlan a;
       it.offE = a.take((size_t)(pl.Mp + pl.Np) * sizeof(int));
       it.offP = a.take((size_t)pl.n_moduli * (pl.Mp + pl.Np) * pl.Kp * 2);
-      it.offR = a.take((size_t)pl.n_moduli * pl.Mp * pl.Np);
+      it.offR = a.take((size_t)pl.n_moduli * pl.Mp * pl.Np * sizeof(uint16_t));
       it.bytes = round_up((int64_t)a.used, 256);
       oz.push_back(it);
     }
@@ -273,14 +273,14 @@ int build(uvatrmm_group_t g, const uvatrmm_trmm_problem *probs, int count) {
       wi.plan = pl;
       wi.LR = reinterpret_cast<uint16_t *>(base + off_wave + it.offP);
       wi.RR = wi.LR + (int64_t)pl.n_moduli * pl.Mp * pl.Kp;
-      wi.res = reinterpret_cast<uint8_t *>(base + off_wave + it.offR);
+      wi.res = reinterpret_cast<uint16_t *>(base + off_wave + it.offR);
       wi.alpha = it.t.alpha;
       wi.C = it.B;
       wi.ldc = it.ldb;
       OzGemmLaunch L;
       L.LR = reinterpret_cast<uint16_t *>(base + off_wave + it.offP);
       L.RR = L.LR + (int64_t)pl.n_moduli * pl.Mp * pl.Kp;
-      L.res = reinterpret_cast<uint8_t *>(base + off_wave + it.offR);
+      L.res = reinterpret_cast<uint16_t *>(base + off_wave + it.offR);
       L.Mp = pl.Mp; L.Np = pl.Np; L.Kp = pl.Kp; L.M = pl.M; L.N = pl.N; L.K = pl.K;
       L.l0 = 0; L.l1 = pl.n_moduli;
       L.tri_left = it.t.side == CblasLeft;

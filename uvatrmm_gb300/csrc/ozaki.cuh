@@ -7,16 +7,19 @@
 //      scale so its entries become integers of at most t bits
 //      (Lft'[i,k] = rint(Lft[i,k] * 2^(t - e_i)), likewise Rgt');
 //   2. slicing  - every integer is cut into its residues modulo N pairwise
-//      coprime moduli m_l <= 256; each residue, balanced into [-128, 128],
-//      is exactly representable in bf16;
+//      coprime moduli m_l <= 363; each residue, balanced into [-181, 181],
+//      is exactly representable in bf16 (integers up to 256 are);
 //   3. products - for every modulus, one bf16 x bf16 -> fp32 tcgen05 GEMM of
-//      the residue matrices.  Products are < 2^14 and every K chunk of 512 is
-//      reduced modulo m_l in the fp32 accumulator (in TMEM) before the next,
-//      so every accumulated value stays below 2^24 and the accumulation is
-//      exact: the kernel yields C' mod m_l exactly;
+//      the residue matrices.  Products are at most 181^2 and every K chunk
+//      of 512 is reduced modulo m_l in the fp32 accumulator (in TMEM) before
+//      the next (512 * 181^2 + 184 < 2^24), so every accumulated value is an
+//      integer below 2^24 and the accumulation is exact: the kernel yields
+//      C' mod m_l exactly, as 16-bit residues;
 //   4. reassembly - the Chinese remainder theorem rebuilds C' (|C'| < M/2,
 //      M = prod m_l, up to 192 bits) per element, which is rounded once to
 //      FP64 and scaled back by 2^(e_i + d_j - 2t) * alpha.
+// Moduli of about 8.4 bits (rather than 8 with m_l <= 256) give the 121 bits
+// that 54-bit entries need at K = 32768 with 15 products instead of 16.
 // N (the slice count) sets M and hence t; see ozaki_bits().
 #pragma once
 
@@ -29,10 +32,11 @@
 namespace uvt {
 
 constexpr int kMaxModuli = 20;
-// Pairwise coprime, largest first: 2^8, 3*5*17, 11*23, 251, 13*19, 241, 239,
-// 233, 229, 227, 223, 7*31, 211, 199, 197, 193, 191, 181, 179, 173.
-constexpr int kModuli[kMaxModuli] = {256, 255, 253, 251, 247, 241, 239, 233, 229, 227,
-                                     223, 217, 211, 199, 197, 193, 191, 181, 179, 173};
+// Pairwise coprime, largest first (greedy from 363 down): 3*11^2, 2*181, 19^2,
+// 359, 5*71, 353, 349, 347, 7^3, 337, 331, 317, 313, 311, 307, 13*23, 293,
+// 17^2, 283, 281.
+constexpr int kModuli[kMaxModuli] = {363, 362, 361, 359, 355, 353, 349, 347, 343, 337,
+                                     331, 317, 313, 311, 307, 299, 293, 289, 283, 281};
 
 // Bits t kept per scaled operand entry for n moduli and inner dimension K:
 // the largest t with K * 2^(2t) < M / 4.
@@ -71,8 +75,8 @@ int oz_scales(const OzOperand &op, int *e, cudaStream_t st);
 int oz_residues(const OzOperand &op, const int *e, int bits, int l0, int l1, int64_t Pp, int64_t Kp, uint16_t *R,
                 cudaStream_t st);
 // CRT reassembly of C (column-major, ldc) from residue planes
-// res[l][j][i] (uint8, plane stride Mp*Np, ld Mp).
-int oz_reassemble(const OzPlan &plan, const uint8_t *res, const int *e_row, const int *e_col, double alpha,
+// res[l][j][i] (uint16, plane stride Mp*Np, ld Mp).
+int oz_reassemble(const OzPlan &plan, const uint16_t *res, const int *e_row, const int *e_col, double alpha,
                   double *C, int64_t ldc, cudaStream_t st);
 
 // Grouped slicing and reassembly for a wave of problems (one launch per
@@ -83,7 +87,7 @@ struct OzWaveItem {
   int *e_row, *e_col;
   OzPlan plan;
   uint16_t *LR, *RR;
-  const uint8_t *res;
+  const uint16_t *res;
   double alpha;
   double *C;
   int64_t ldc;
@@ -109,7 +113,7 @@ int oz_wave_reassemble(const OzWaveTables &t, cudaStream_t st);
 struct OzGroupProb;
 struct OzGemmLaunch {
   const uint16_t *LR, *RR;
-  uint8_t *res;
+  uint16_t *res;
   int64_t Mp, Np, Kp, M, N, K;
   int l0, l1;
   bool tri_left, tri_lower;
@@ -128,7 +132,7 @@ struct alignas(128) OzGroupProb {
   int l0, l1;
   int tri_left, tri_lower, grows;
   int tiles_m, tiles_n, tiles_per_mod, group;
-  uint8_t *res;
+  uint16_t *res;
   int64_t plane;
   int tile_begin, tile_count;
   int tile_offset;  // first of the problem's own tiles this launch covers

@@ -61,7 +61,8 @@ int ozaki_device(uvatrmm_handle_t h, int layout, int side, int uplo, int transa,
   int G = (int)std::max<int64_t>(1, std::min<int64_t>(plan.n_moduli, (h->ozaki_scratch_mb << 20) / per_mod));
   const size_t e_bytes = (size_t)round_up((plan.Mp + plan.Np) * (int64_t)sizeof(int), 256);
   int *e = static_cast<int *>(workspace(h, 4, e_bytes + sizeof(OzGroupProb)));
-  uint8_t *res = static_cast<uint8_t *>(workspace(h, 6, (size_t)plan.n_moduli * plan.Mp * plan.Np));
+  uint16_t *res =
+      static_cast<uint16_t *>(workspace(h, 6, (size_t)plan.n_moduli * plan.Mp * plan.Np * sizeof(uint16_t)));
   uint16_t *planes = static_cast<uint16_t *>(workspace(h, 5, (size_t)G * per_mod));
   if (!e || !res || !planes) return uvatrmm_last_status();
   int *e_row = e, *e_col = e + plan.Mp;

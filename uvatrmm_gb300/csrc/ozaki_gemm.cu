@@ -8,9 +8,11 @@
 // modulo m_l in place (tcgen05.ld -> fp32 fold -> tcgen05.st) while the MMA
 // thread fills the other TMEM accumulator with the next chunk; the next chunk
 // for that accumulator then adds on top of the folded value.  Residues are
-// <= 128 in magnitude, so every value the accumulator ever holds is an
-// integer below 2^24 and fp32 accumulation is exact.  The last two chunks
-// are combined and the tile's residues (0 <= r < m_l) are written as bytes.
+// at most 181 in magnitude (moduli up to 363) and a folded value at most a
+// few units past m/2, so every value the accumulator ever holds is an
+// integer below 512 * 181^2 + 184 < 2^24 and fp32 accumulation is exact.
+// The last two chunks are combined and the tile's residues (0 <= r < m_l)
+// are written as 16-bit words.
 //
 // CTA pairs.  The kernel runs in clusters of two CTAs stacked along M: the
 // pair computes a 256 x 256 block (rows 2*tp*128 + rank*128 for each CTA)
@@ -22,9 +24,10 @@
 // on the stage's empty barrier in both CTAs.
 //
 // The accumulators alternate across tiles (chunk g of a CTA uses buffer
-// g & 1).  The second-to-last chunk of a tile is reduced to byte residues in
-// shared memory and its buffer released at once, so the next
-// tile's first chunk runs while the last chunk is combined and stored.
+// g & 1).  The second-to-last chunk of a tile is reduced to residues (low
+// bytes in shared memory, the ninth bits in a per-thread word per 32
+// columns) and its buffer released at once, so the next tile's first chunk
+// runs while the last chunk is combined and stored.
 //
 // Warp roles (192 threads, one CTA per SM): warp 0 TMA producer, warp 1 TMEM
 // owner + MMA issuer, warps 2-5 epilogue (each bound to its TMEM lane
@@ -51,7 +54,7 @@ constexpr uint32_t A_BYTES = BM * BK * 2, B_BYTES = BN * BK * 2, BH_BYTES = BH *
 constexpr uint32_t STAGE_BYTES = A_BYTES + B_BYTES;
 constexpr int NUM_THREADS = 192;
 constexpr uint32_t TMEM_COLS = 2 * BN;  // two fp32 accumulators of 256 columns
-// Byte residues of a tile's second-to-last chunk, [column word][row] (32 KB).
+// Low bytes of a tile's second-to-last chunk residues, [column word][row] (32 KB).
 constexpr uint32_t R1_BYTES = BM * BN;
 constexpr size_t SMEM = 1024 + (size_t)STAGES * STAGE_BYTES + 256 + R1_BYTES;
 // kind::f16 instruction descriptor: D fp32 (bits 4-5 = 1), A and B bf16
@@ -357,7 +360,10 @@ __global__ void __cluster_dims__(PAIR, 1, 1) __launch_bounds__(NUM_THREADS, 1)
       const int nslab = T.ks1 - T.ks0;
       const int nchunk = (nslab + CHUNK_SLABS - 1) / CHUNK_SLABS;
       const float m = p.mod_f[T.l], inv = p.inv_f[T.l];
+      // This thread's row of the tile's residue output (column stride Mp).
+      uint16_t *out = P.res + (int64_t)T.l * P.plane + ((int64_t)T.tp * PAIR + rank) * BM + row;
       uint32_t *r1 = r1s + row;  // this row's words of r1s, stride BM (each thread touches only its own)
+      uint32_t hib[BN / 32];     // ninth bits of the second-to-last chunk's residues
       for (int c = 0; c < nchunk; ++c, ++gc) {
         const uint32_t b = gc & 1u, u = gc >> 1;
         if (!mbar_wait_bounded(&cdone[b], u & 1u)) {
@@ -383,40 +389,45 @@ __global__ void __cluster_dims__(PAIR, 1, 1) __launch_bounds__(NUM_THREADS, 1)
           }
           tmem_wait_st();
         } else if (c + 2 == nchunk) {
-          // Second-to-last chunk: its residues move to shared memory, the buffer is freed now.
+          // Second-to-last chunk: its residues move aside, the buffer is freed now.
 #pragma unroll 1
           for (int cb = 0; cb < BN / 32; ++cb) {
             uint32_t v[32];
             tmem_ld32(tb + (uint32_t)(cb * 32), v);
             tmem_wait_ld();
+            uint32_t hi = 0;
 #pragma unroll
             for (int q = 0; q < 8; ++q) {
               uint32_t w = 0;
 #pragma unroll
-              for (int e = 0; e < 4; ++e)
-                w |= (uint32_t)(int)mod_pos(__uint_as_float(v[q * 4 + e]), m, inv) << (8 * e);
+              for (int e = 0; e < 4; ++e) {
+                const uint32_t r = (uint32_t)(int)mod_pos(__uint_as_float(v[q * 4 + e]), m, inv);
+                w |= (r & 255u) << (8 * e);
+                hi |= (r >> 8) << (q * 4 + e);
+              }
               r1[(cb * 8 + q) * BM] = w;
             }
+            hib[cb] = hi;
           }
         } else {
-          // Last chunk: residue of (this chunk + the second-to-last) as bytes.
+          // Last chunk: residue of (this chunk + the second-to-last) as 16-bit words.
           const bool two = nchunk >= 2;
-          const int64_t i = ((int64_t)T.tp * PAIR + rank) * BM + row;
-          uint8_t *out = P.res + (int64_t)T.l * P.plane + i;
 #pragma unroll 1
           for (int cb = 0; cb < BN / 32; ++cb) {
             uint32_t v[32];
             tmem_ld32(tb + (uint32_t)(cb * 32), v);
             tmem_wait_ld();
             const int64_t j0 = (int64_t)T.tj * BN + cb * 32;
+            const uint32_t hi = two ? hib[cb] : 0u;
 #pragma unroll
             for (int q = 0; q < 8; ++q) {
               const uint32_t w = two ? r1[(cb * 8 + q) * BM] : 0u;
 #pragma unroll
               for (int e = 0; e < 4; ++e) {
-                float r = mod_pos(__uint_as_float(v[q * 4 + e]), m, inv) + (float)((w >> (8 * e)) & 255u);
+                const uint32_t prev = ((w >> (8 * e)) & 255u) | (((hi >> (q * 4 + e)) & 1u) << 8);
+                float r = mod_pos(__uint_as_float(v[q * 4 + e]), m, inv) + (float)prev;
                 if (r >= m) r -= m;
-                out[(j0 + q * 4 + e) * P.Mp] = (uint8_t)(int)r;
+                out[(j0 + q * 4 + e) * P.Mp] = (uint16_t)(int)r;
               }
             }
           }

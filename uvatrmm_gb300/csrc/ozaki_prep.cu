@@ -114,12 +114,12 @@ __device__ __forceinline__ void store_residues(const uint32_t (&w)[4], bool neg,
 
 // Integers below 2^63 (every automatic slice count) go through the FP32
 // pipe: x = sum_i d_i 2^(11 i) with six 11-bit digits, so x is congruent to
-// s = sum_i d_i (2^(11 i) mod m) < 6 * 2^11 * 2^8 < 2^22 modulo m, exact in
+// s = sum_i d_i (2^(11 i) mod m) < 6 * 2^11 * 363 < 2^23 modulo m, exact in
 // fp32.  r = s - m * rint(s / m), rounding by the 1.5 * 2^23 constant in one
-// fma, is congruent to x; the quotient's error (below 0.002) can only move a
-// remainder sitting at +-(m-1)/2 to -+(m+1)/2, so |r| <= 128 as the residue
-// GEMM's exactness bound requires.  The balanced representative may differ
-// from the integer path's at that tie, never its class modulo m.
+// fma, is congruent to x: the quotient's error, at most (s/m) 2^-24 < 0.00074,
+// is below the gap 1/(2m) between s/m and a half-integer for the odd moduli,
+// and the even modulus 362 only has the tie +-181 either way, so |r| <= 181
+// as the residue GEMM's exactness bound requires.
 
 // Digits d_0 .. d_5 of x as exact floats.
 __device__ __forceinline__ void digits11(uint64_t x, float (&d)[6]) {
@@ -144,7 +144,7 @@ __device__ __forceinline__ uint32_t residue_bits(const float (&d)[6]) {
   s = fmaf(d[5], c5, s);
   const float q = fmaf(s, inv, 12582912.0f) - 12582912.0f;
   const float r = fmaf(-q, mf, s);
-  return __float_as_uint(r) >> 16;  // |r| <= 128: exact in bf16
+  return __float_as_uint(r) >> 16;  // |r| <= 181: exact in bf16
 }
 
 // Residues of four consecutive-k entries for moduli [l0, l1), one 8-byte
@@ -238,8 +238,8 @@ __global__ void __launch_bounds__(256) residue_kernel(OzOperand op, const int *e
 }
 
 // ---------------------------------------------------------------- reassembly
-// 32-bit limbs, least significant first.  S = sum_l r_l W_l < 20 * 2^8 * M
-// needs 6 limbs for 20 moduli (M < 2^157).
+// 32-bit limbs, least significant first.  S = sum_l r_l W_l < 20 * 363 * M
+// needs 6 limbs for 20 moduli (M < 2^167, S < 2^180).
 constexpr int kLimbs = 6;
 
 struct CrtConst {
@@ -282,8 +282,8 @@ __device__ __forceinline__ double times_pow2(double d, int k) {
   return ldexp(d, k);
 }
 
-// One element: residues r_l (byte `sh` of rw[l]) -> C value (alpha applied).
-__device__ __forceinline__ double crt_element(const CrtConst &cc, const uint32_t (&rw)[kMaxModuli], int sh, int er,
+// One element: residues r_l (16-bit field `f` of the pair rw[l]) -> C value (alpha applied).
+__device__ __forceinline__ double crt_element(const CrtConst &cc, const uint2 (&rw)[kMaxModuli], int f, int er,
                                               int ec, double alpha, bool unit_alpha) {
   // S = sum_l r_l W_l: per-limb 64-bit sums (each < 20 * 2^40), carries once.
   uint64_t acc[kLimbs];
@@ -292,7 +292,7 @@ __device__ __forceinline__ double crt_element(const CrtConst &cc, const uint32_t
 #pragma unroll
   for (int l = 0; l < kMaxModuli; ++l) {
     if (l < cc.n) {
-      const uint32_t r = (rw[l] >> sh) & 255u;
+      const uint32_t r = ((f < 2 ? rw[l].x : rw[l].y) >> (16 * (f & 1))) & 0xFFFFu;
 #pragma unroll
       for (int k = 0; k < kLimbs; ++k) acc[k] += (uint64_t)r * cc.W[l][k];
     }
@@ -388,34 +388,37 @@ __device__ __forceinline__ double crt_element(const CrtConst &cc, const uint32_t
 }
 
 // Rows [1024 bx, 1024 bx + 1024) of columns j0, j0 + jstep, ... of C; each
-// thread takes four consecutive rows (one 4-byte load per residue plane).
-__device__ __forceinline__ void reassemble_body(const CrtConst &cc, const uint8_t *res, int64_t Mp, int64_t plane,
+// thread takes four consecutive rows (one 8-byte load per residue plane).
+constexpr int kCrtRows = 4;
+
+__device__ __forceinline__ void reassemble_body(const CrtConst &cc, const uint16_t *res, int64_t Mp, int64_t plane,
                                                 int64_t M, int64_t N, const int *e_row, const int *e_col,
                                                 double alpha, double *C, int64_t ldc, int64_t bx, int64_t j0,
                                                 int64_t jstep) {
-  const int64_t i0 = (bx * blockDim.x + threadIdx.x) * 4;
+  const int64_t i0 = (bx * blockDim.x + threadIdx.x) * kCrtRows;
   if (i0 >= M) return;
   const bool unit_alpha = alpha == 1.0;
   const int4 er4 = *reinterpret_cast<const int4 *>(e_row + i0);
-  const int er[4] = {er4.x, er4.y, er4.z, er4.w};
+  const int er[kCrtRows] = {er4.x, er4.y, er4.z, er4.w};
   for (int64_t j = j0; j < N; j += jstep) {
     const int ec = e_col[j];
-    uint32_t rw[kMaxModuli];
-    const uint8_t *rp = res + j * Mp + i0;
+    uint2 rw[kMaxModuli];
+    const uint16_t *rp = res + j * Mp + i0;
 #pragma unroll
-    for (int l = 0; l < kMaxModuli; ++l) rw[l] = l < cc.n ? *reinterpret_cast<const uint32_t *>(rp + l * plane) : 0u;
+    for (int l = 0; l < kMaxModuli; ++l)
+      rw[l] = l < cc.n ? *reinterpret_cast<const uint2 *>(rp + l * plane) : make_uint2(0u, 0u);
 #pragma unroll
-    for (int q = 0; q < 4; ++q) {
+    for (int q = 0; q < kCrtRows; ++q) {
       if (i0 + q >= M) break;
       double v;
       if (er[q] == kExpNone || ec == kExpNone) v = alpha * 0.0;
-      else v = crt_element(cc, rw, 8 * q, er[q], ec, alpha, unit_alpha);
+      else v = crt_element(cc, rw, q, er[q], ec, alpha, unit_alpha);
       C[i0 + q + j * ldc] = v;
     }
   }
 }
 
-__global__ void __launch_bounds__(256) reassemble_kernel(const __grid_constant__ CrtConst cc, const uint8_t *res,
+__global__ void __launch_bounds__(256) reassemble_kernel(const __grid_constant__ CrtConst cc, const uint16_t *res,
                                                          int64_t Mp, int64_t plane, int64_t M, int64_t N,
                                                          const int *e_row, const int *e_col, double alpha,
                                                          double *C, int64_t ldc) {
@@ -440,7 +443,7 @@ struct ResidueJob {
 };
 struct CrtJob {
   CrtConst cc;
-  const uint8_t *res;
+  const uint16_t *res;
   int64_t Mp, plane, M, N, gx;
   const int *e_row, *e_col;
   double alpha;
@@ -648,7 +651,7 @@ void oz_wave_image(const OzWaveItem *items, int n, void *dev, std::vector<char> 
     c.plane = pl.Mp * pl.Np;
     c.M = pl.M;
     c.N = pl.N;
-    c.gx = (pl.M + 1023) / 1024;
+    c.gx = (pl.M + 256 * kCrtRows - 1) / (256 * kCrtRows);
     c.e_row = it.e_row;
     c.e_col = it.e_col;
     c.alpha = it.alpha;
@@ -690,11 +693,11 @@ int oz_wave_reassemble(const OzWaveTables &t, cudaStream_t st) {
   return cudaGetLastError() == cudaSuccess ? UVATRMM_OK : UVATRMM_EDEVICE;
 }
 
-int oz_reassemble(const OzPlan &plan, const uint8_t *res, const int *e_row, const int *e_col, double alpha,
+int oz_reassemble(const OzPlan &plan, const uint16_t *res, const int *e_row, const int *e_col, double alpha,
                   double *C, int64_t ldc, cudaStream_t st) {
   const CrtConst cc = make_crt(plan);
   if (plan.M <= 0 || plan.N <= 0) return UVATRMM_OK;
-  dim3 grid((unsigned)((plan.M + 1023) / 1024), (unsigned)std::min<int64_t>(plan.N, 65535));
+  dim3 grid((unsigned)((plan.M + 256 * kCrtRows - 1) / (256 * kCrtRows)), (unsigned)std::min<int64_t>(plan.N, 65535));
   reassemble_kernel<<<grid, 256, 0, st>>>(cc, res, plan.Mp, plan.Mp * plan.Np, plan.M, plan.N, e_row, e_col,
                                            alpha, C, ldc);
   return cudaGetLastError() == cudaSuccess ? UVATRMM_OK : UVATRMM_EDEVICE;

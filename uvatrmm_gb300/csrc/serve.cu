@@ -121,7 +121,7 @@ struct Req {
   OzGroupProb od{};
   int *e_row = nullptr, *e_col = nullptr;
   uint16_t *LR = nullptr, *RR = nullptr;
-  uint8_t *res = nullptr;
+  uint16_t *res = nullptr;
   bool prepped = false;
   // tile progress
   int total = 0, next = 0;
@@ -191,7 +191,7 @@ size_t working_bytes(const Req &r) {
     if (!r.on_device) add((size_t)round_up(t.m, 16) * t.n * 8);  // B copy, overwritten
     add((size_t)(pl.Mp + pl.Np) * sizeof(int));
     add((size_t)pl.n_moduli * (pl.Mp + pl.Np) * pl.Kp * 2);
-    add((size_t)pl.n_moduli * pl.Mp * pl.Np);
+    add((size_t)pl.n_moduli * pl.Mp * pl.Np * sizeof(uint16_t));
   }
   return b;
 }
@@ -287,7 +287,7 @@ int setup(uvatrmm_server_t s, Req &r) {
     r.e_col = r.e_row + pl.Mp;
     r.LR = reinterpret_cast<uint16_t *>(take((size_t)pl.n_moduli * (pl.Mp + pl.Np) * pl.Kp * 2));
     r.RR = r.LR + (int64_t)pl.n_moduli * pl.Mp * pl.Kp;
-    r.res = reinterpret_cast<uint8_t *>(take((size_t)pl.n_moduli * pl.Mp * pl.Np));
+    r.res = reinterpret_cast<uint16_t *>(take((size_t)pl.n_moduli * pl.Mp * pl.Np * sizeof(uint16_t)));
     OzGemmLaunch L;
     L.LR = r.LR;
     L.RR = r.RR;
