@@ -283,6 +283,7 @@ int build(uvatrmm_group_t g, const uvatrmm_trmm_problem *probs, int count) {
       L.res = reinterpret_cast<uint16_t *>(base + off_wave + it.offR);
       L.Mp = pl.Mp; L.Np = pl.Np; L.Kp = pl.Kp; L.M = pl.M; L.N = pl.N; L.K = pl.K;
       L.l0 = 0; L.l1 = pl.n_moduli;
+      L.n_moduli = pl.n_moduli;
       L.tri_left = it.t.side == CblasLeft;
       L.tri_lower = (it.t.uplo == CblasLower) != (it.t.trans != 0);
       L.raster_group = it.raster;

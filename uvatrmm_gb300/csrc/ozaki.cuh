@@ -13,11 +13,13 @@
 //      the residue matrices.  Products are at most 181^2 and every K chunk
 //      of 512 is reduced modulo m_l in the fp32 accumulator (in TMEM) before
 //      the next (512 * 181^2 + 184 < 2^24), so every accumulated value is an
-//      integer below 2^24 and the accumulation is exact: the kernel yields
-//      C' mod m_l exactly, as 16-bit residues;
-//   4. reassembly - the Chinese remainder theorem rebuilds C' (|C'| < M/2,
-//      M = prod m_l, up to 192 bits) per element, which is rounded once to
-//      FP64 and scaled back by 2^(e_i + d_j - 2t) * alpha.
+//      integer below 2^24 and the accumulation is exact.  The kernel stores
+//      y_l = u_l C' mod m_l as 16-bit words, u_l = (M/m_l)^-1 mod m_l
+//      (M = prod m_l);
+//   4. reassembly - the Chinese remainder theorem rebuilds C' (|C'| < M/4)
+//      per element as S - k M with S = sum_l y_l (M/m_l) and k = rint(S/M),
+//      which is rounded once to FP64 and scaled back by
+//      2^(e_i + d_j - 2t) * alpha.
 // Moduli of about 8.4 bits (rather than 8 with m_l <= 256) give the 121 bits
 // that 54-bit entries need at K = 32768 with 15 products instead of 16.
 // N (the slice count) sets M and hence t; see ozaki_bits().
@@ -37,6 +39,21 @@ constexpr int kMaxModuli = 20;
 // 17^2, 283, 281.
 constexpr int kModuli[kMaxModuli] = {363, 362, 361, 359, 355, 353, 349, 347, 343, 337,
                                      331, 317, 313, 311, 307, 299, 293, 289, 283, 281};
+
+// u_l = (M/m_l)^-1 mod m_l for the first n moduli, M = prod_{j<n} m_j.
+constexpr int crt_u(int n, int l) {
+  const int m = kModuli[l];
+  int prod = 1;
+  for (int j = 0; j < n; ++j)
+    if (j != l) prod = prod * (kModuli[j] % m) % m;
+  // Extended Euclid: prod * u = 1 (mod m).
+  int r0 = m, r1 = prod, t0 = 0, t1 = 1;
+  while (r1) {
+    const int q = r0 / r1, r2 = r0 - q * r1, t2 = t0 - q * t1;
+    r0 = r1; r1 = r2; t0 = t1; t1 = t2;
+  }
+  return t0 < 0 ? t0 + m : t0;
+}
 
 // Bits t kept per scaled operand entry for n moduli and inner dimension K:
 // the largest t with K * 2^(2t) < M / 4.
@@ -116,6 +133,7 @@ struct OzGemmLaunch {
   uint16_t *res;
   int64_t Mp, Np, Kp, M, N, K;
   int l0, l1;
+  int n_moduli = 0;  // moduli of the CRT set (sets u_l of the stored residues)
   bool tri_left, tri_lower;
   int raster_group = 0;          // major tiles per raster group (0 = default, 2)
   OzGroupProb *desc = nullptr;   // device slot for the descriptor (single launches)
@@ -136,6 +154,7 @@ struct alignas(128) OzGroupProb {
   int64_t plane;
   int tile_begin, tile_count;
   int tile_offset;  // first of the problem's own tiles this launch covers
+  int nmod;         // moduli of the problem's CRT set
 };
 // Fills the descriptor of one residue GEMM (tile_begin left to the caller).
 int oz_group_prob(const OzGemmLaunch &L, OzGroupProb *out, const char **why);

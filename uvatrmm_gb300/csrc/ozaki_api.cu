@@ -113,6 +113,7 @@ int ozaki_device(uvatrmm_handle_t h, int layout, int side, int uplo, int transa,
     g.Mp = plan.Mp; g.Np = plan.Np; g.Kp = plan.Kp;
     g.M = plan.M; g.N = plan.N; g.K = plan.K;
     g.l0 = l0; g.l1 = l1;
+    g.n_moduli = plan.n_moduli;
     g.tri_left = t.side == CblasLeft;
     g.tri_lower = (t.uplo == CblasLower) != (t.trans != 0);
     g.status = h->dctl + 1;

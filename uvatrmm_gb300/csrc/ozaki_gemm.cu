@@ -68,6 +68,7 @@ struct GParams {
   int *status;
   float mod_f[kMaxModuli];
   float inv_f[kMaxModuli];
+  float u_f[kMaxModuli + 1][kMaxModuli];  // u_f[n][l] = crt_u(n, l)
 };
 
 struct Tile {
@@ -359,7 +360,7 @@ __global__ void __cluster_dims__(PAIR, 1, 1) __launch_bounds__(NUM_THREADS, 1)
       const Tile T = decode(P, t - P.tile_begin + P.tile_offset);
       const int nslab = T.ks1 - T.ks0;
       const int nchunk = (nslab + CHUNK_SLABS - 1) / CHUNK_SLABS;
-      const float m = p.mod_f[T.l], inv = p.inv_f[T.l];
+      const float m = p.mod_f[T.l], inv = p.inv_f[T.l], cu = p.u_f[P.nmod][T.l];
       // This thread's row of the tile's residue output (column stride Mp).
       uint16_t *out = P.res + (int64_t)T.l * P.plane + ((int64_t)T.tp * PAIR + rank) * BM + row;
       uint32_t *r1 = r1s + row;  // this row's words of r1s, stride BM (each thread touches only its own)
@@ -410,7 +411,11 @@ __global__ void __cluster_dims__(PAIR, 1, 1) __launch_bounds__(NUM_THREADS, 1)
             hib[cb] = hi;
           }
         } else {
-          // Last chunk: residue of (this chunk + the second-to-last) as 16-bit words.
+          // Last chunk: with v this chunk's sum and p the parked residue, the
+          // stored 16-bit word is u_l (v + p) mod m_l.  v is folded to
+          // |v'| <= 184 first, so x = (v' + p) u_l has |x| < 546 * 362 < 2^18
+          // (exact); floor(x / m) in fp32 is exact except that a multiple of m
+          // may come out one low, which the single correction handles.
           const bool two = nchunk >= 2;
 #pragma unroll 1
           for (int cb = 0; cb < BN / 32; ++cb) {
@@ -425,9 +430,11 @@ __global__ void __cluster_dims__(PAIR, 1, 1) __launch_bounds__(NUM_THREADS, 1)
 #pragma unroll
               for (int e = 0; e < 4; ++e) {
                 const uint32_t prev = ((w >> (8 * e)) & 255u) | (((hi >> (q * 4 + e)) & 1u) << 8);
-                float r = mod_pos(__uint_as_float(v[q * 4 + e]), m, inv) + (float)prev;
-                if (r >= m) r -= m;
-                out[(j0 + q * 4 + e) * P.Mp] = (uint16_t)(int)r;
+                const float a = __uint_as_float(v[q * 4 + e]);
+                const float x = (fmaf(-rintf(a * inv), m, a) + (float)prev) * cu;
+                float y = fmaf(-floorf(x * inv), m, x);
+                if (y >= m) y -= m;
+                out[(j0 + q * 4 + e) * P.Mp] = (uint16_t)(int)y;
               }
             }
           }
@@ -464,6 +471,10 @@ int oz_group_prob(const OzGemmLaunch &L, OzGroupProb *out, const char **why) {
     *why = "residue planes are not padded to the tile sizes";
     return UVATRMM_EINVAL;
   }
+  if (L.l0 < 0 || L.l1 > L.n_moduli || L.n_moduli > kMaxModuli) {
+    *why = "residue GEMM moduli outside the CRT set";
+    return UVATRMM_EINVAL;
+  }
   const int nmod = L.l1 - L.l0;
   if ((int64_t)nmod * L.Mp > INT32_MAX || (int64_t)nmod * L.Np > INT32_MAX || L.Kp > INT32_MAX) {
     *why = "problem too large for one residue pass";
@@ -488,6 +499,7 @@ int oz_group_prob(const OzGemmLaunch &L, OzGroupProb *out, const char **why) {
   out->group = L.raster_group > 0 ? L.raster_group : 2;
   out->res = L.res;
   out->plane = L.Mp * L.Np;
+  out->nmod = L.n_moduli;
   return UVATRMM_OK;
 }
 
@@ -526,6 +538,7 @@ int launch_oz_gemm_group(const OzGroupProb *dprobs, int nprob, int total_tiles, 
   for (int l = 0; l < kMaxModuli; ++l) {
     g.mod_f[l] = (float)kModuli[l];
     g.inv_f[l] = 1.0f / (float)kModuli[l];
+    for (int n = l + 1; n <= kMaxModuli; ++n) g.u_f[n][l] = (float)crt_u(n, l);
   }
   if (oz_gemm_prepare() != UVATRMM_OK) {
     *why = "cannot reserve shared memory for the residue GEMM";

@@ -238,43 +238,22 @@ __global__ void __launch_bounds__(256) residue_kernel(OzOperand op, const int *e
 }
 
 // ---------------------------------------------------------------- reassembly
-// 32-bit limbs, least significant first.  S = sum_l r_l W_l < 20 * 363 * M
-// needs 6 limbs for 20 moduli (M < 2^167, S < 2^180).
-constexpr int kLimbs = 6;
+// The residue GEMM stores y_l = u_l C' mod m_l (0 <= y_l < m_l), so
+// S = sum_l y_l P_l with P_l = M/m_l is congruent to C' modulo M and
+// S/M = sum_l y_l/m_l < n.  With |C'| <= K 2^(2t) < M/4, C' = S - k M for
+// k = rint(S/M), and any estimate of S/M within 1/4 gives that k.  C' is
+// formed in L 32-bit limbs (least significant first) in two's complement,
+// M < 2^(32L), so limbs above L never matter.  S's limb sums are < 20 * 363 * 2^32.
+constexpr int kLimbs = 6;  // L for 20 moduli (M < 2^168)
 
 struct CrtConst {
   int n;
   int bits;
-  int base;                        // quotient estimate reads limbs base .. base+2
-  float inv_mf;                    // 2^(32 base) / M
-  uint32_t W[kMaxModuli][kLimbs];  // W_l = (M/m_l) * ((M/m_l)^-1 mod m_l)
-  uint32_t Mw[kLimbs], halfM[kLimbs];
+  int limbs;                       // L
+  float c_hi, c_lo;                // 2^(32(L-1)) / M, 2^(32(L-2)) / M
+  uint32_t P[kMaxModuli][kLimbs];  // P_l = M / m_l
+  uint32_t Mw[kLimbs];
 };
-
-__device__ __forceinline__ bool lt6(const uint32_t (&a)[kLimbs], const uint32_t (&b)[kLimbs]) {
-#pragma unroll
-  for (int k = kLimbs - 1; k >= 0; --k)
-    if (a[k] != b[k]) return a[k] < b[k];
-  return false;
-}
-__device__ __forceinline__ void sub6(uint32_t (&a)[kLimbs], const uint32_t (&b)[kLimbs]) {
-  uint32_t br = 0;
-#pragma unroll
-  for (int k = 0; k < kLimbs; ++k) {
-    const uint64_t t = (uint64_t)a[k] - b[k] - br;
-    a[k] = (uint32_t)t;
-    br = (uint32_t)(t >> 63);
-  }
-}
-__device__ __forceinline__ void add6(uint32_t (&a)[kLimbs], const uint32_t (&b)[kLimbs]) {
-  uint64_t c = 0;
-#pragma unroll
-  for (int k = 0; k < kLimbs; ++k) {
-    c += (uint64_t)a[k] + b[k];
-    a[k] = (uint32_t)c;
-    c >>= 32;
-  }
-}
 
 // d * 2^k, exact when the result is a normal double.
 __device__ __forceinline__ double times_pow2(double d, int k) {
@@ -282,79 +261,64 @@ __device__ __forceinline__ double times_pow2(double d, int k) {
   return ldexp(d, k);
 }
 
-// One element: residues r_l (16-bit field `f` of the pair rw[l]) -> C value (alpha applied).
+// One element from its residues (16-bit field `f` of the pairs rw[l]) -> C value (alpha applied).
+template <int L>
 __device__ __forceinline__ double crt_element(const CrtConst &cc, const uint2 (&rw)[kMaxModuli], int f, int er,
                                               int ec, double alpha, bool unit_alpha) {
-  // S = sum_l r_l W_l: per-limb 64-bit sums (each < 20 * 2^40), carries once.
-  uint64_t acc[kLimbs];
+  uint64_t acc[L];
 #pragma unroll
-  for (int k = 0; k < kLimbs; ++k) acc[k] = 0;
+  for (int k = 0; k < L; ++k) acc[k] = 0;
 #pragma unroll
   for (int l = 0; l < kMaxModuli; ++l) {
     if (l < cc.n) {
-      const uint32_t r = ((f < 2 ? rw[l].x : rw[l].y) >> (16 * (f & 1))) & 0xFFFFu;
+      const uint32_t y = ((f < 2 ? rw[l].x : rw[l].y) >> (16 * (f & 1))) & 0xFFFFu;
 #pragma unroll
-      for (int k = 0; k < kLimbs; ++k) acc[k] += (uint64_t)r * cc.W[l][k];
+      for (int k = 0; k < L; ++k) acc[k] += (uint64_t)y * cc.P[l][k];
     }
   }
-  uint32_t S[kLimbs];
-  uint64_t c = 0;
+  // k from the two top limb sums: the limbs below add less than 2^-20 to S/M
+  // and the fp32 rounding stays below 2^-18.
+  const float sm = fmaf((float)acc[L - 1], cc.c_hi, (float)acc[L - 2] * cc.c_lo);
+  const uint32_t kq = (uint32_t)(sm + 0.5f);
+  // X = S - k M in two's complement, then sign and magnitude.
+  uint32_t X[L];
+  int64_t c = 0;
 #pragma unroll
-  for (int k = 0; k < kLimbs; ++k) {
-    c += acc[k];
-    S[k] = (uint32_t)c;
+  for (int k = 0; k < L; ++k) {
+    c += (int64_t)acc[k] - (int64_t)((uint64_t)kq * cc.Mw[k]);
+    X[k] = (uint32_t)c;
     c >>= 32;
   }
-  // R = S mod M: fp32 quotient estimate (off by at most one), then one
-  // correction each way.
-  float sf = 0.f;
-#pragma unroll
-  for (int k = kLimbs - 1; k >= 0; --k)
-    if (k >= cc.base && k <= cc.base + 2) sf = fmaf(sf, 4294967296.0f, (float)S[k]);
-  const uint32_t q = (uint32_t)floorf(sf * cc.inv_mf);
-  uint32_t qM[kLimbs];
-  {
-    uint64_t t = 0;
-#pragma unroll
-    for (int k = 0; k < kLimbs; ++k) {
-      t += (uint64_t)q * cc.Mw[k];
-      qM[k] = (uint32_t)t;
-      t >>= 32;
-    }
-  }
-  if (lt6(S, qM)) add6(S, cc.Mw);  // estimate one too high
-  sub6(S, qM);
-  if (!lt6(S, cc.Mw)) sub6(S, cc.Mw);  // estimate one too low
-  // Signed value in (-M/2, M/2].
-  const bool neg = lt6(cc.halfM, S);
+  const bool neg = (X[L - 1] >> 31) != 0;
   if (neg) {
-    uint32_t t[kLimbs];
+    uint32_t cy = 1;
 #pragma unroll
-    for (int k = 0; k < kLimbs; ++k) t[k] = cc.Mw[k];
-    sub6(t, S);
-#pragma unroll
-    for (int k = 0; k < kLimbs; ++k) S[k] = t[k];
+    for (int k = 0; k < L; ++k) {
+      const uint64_t t = (uint64_t)(~X[k]) + cy;
+      X[k] = (uint32_t)t;
+      cy = (uint32_t)(t >> 32);
+    }
   }
   // Round the magnitude to FP64 once: a 64-bit window below the top bit,
   // with a sticky bit for everything under it.
   int t = 0;
 #pragma unroll
-  for (int k = 1; k < kLimbs; ++k)
-    if (S[k]) t = k;
+  for (int k = 1; k < L; ++k)
+    if (X[k]) t = k;
   uint64_t top;
   int ex;
   if (t == 0) {
-    top = S[0];
+    top = X[0];
     ex = 0;
   } else {
-    const int lz = __clz(S[t]);
-    const uint64_t w = ((uint64_t)S[t] << 32) | S[t - 1];
-    const uint32_t below = t >= 2 ? S[t - 2] : 0u;
+    const int lz = __clz(X[t]);
+    const uint64_t w = ((uint64_t)X[t] << 32) | X[t - 1];
+    const uint32_t below = t >= 2 ? X[t - 2] : 0u;
     top = lz ? (w << lz) | (below >> (32 - lz)) : w;
     bool sticky = (lz ? (below << lz) : below) != 0u;
 #pragma unroll
-    for (int k = 0; k < kLimbs - 3; ++k)
-      if (k < t - 2 && S[k]) sticky = true;
+    for (int k = 0; k < L - 3; ++k)
+      if (k < t - 2 && X[k]) sticky = true;
     if (t < 2) sticky = false;
     top |= sticky ? 1ull : 0ull;
     ex = 32 * (t - 1) - lz;
@@ -391,6 +355,7 @@ __device__ __forceinline__ double crt_element(const CrtConst &cc, const uint2 (&
 // thread takes four consecutive rows (one 8-byte load per residue plane).
 constexpr int kCrtRows = 4;
 
+template <int L>
 __device__ __forceinline__ void reassemble_body(const CrtConst &cc, const uint16_t *res, int64_t Mp, int64_t plane,
                                                 int64_t M, int64_t N, const int *e_row, const int *e_col,
                                                 double alpha, double *C, int64_t ldc, int64_t bx, int64_t j0,
@@ -407,22 +372,26 @@ __device__ __forceinline__ void reassemble_body(const CrtConst &cc, const uint16
 #pragma unroll
     for (int l = 0; l < kMaxModuli; ++l)
       rw[l] = l < cc.n ? *reinterpret_cast<const uint2 *>(rp + l * plane) : make_uint2(0u, 0u);
-#pragma unroll
+    // One row at a time: interleaving the four rows' limb sums doubles the
+    // registers and halves the resident blocks.
+#pragma unroll 1
     for (int q = 0; q < kCrtRows; ++q) {
       if (i0 + q >= M) break;
+      const int erq = q == 0 ? er[0] : q == 1 ? er[1] : q == 2 ? er[2] : er[3];
       double v;
-      if (er[q] == kExpNone || ec == kExpNone) v = alpha * 0.0;
-      else v = crt_element(cc, rw, q, er[q], ec, alpha, unit_alpha);
+      if (erq == kExpNone || ec == kExpNone) v = alpha * 0.0;
+      else v = crt_element<L>(cc, rw, q, erq, ec, alpha, unit_alpha);
       C[i0 + q + j * ldc] = v;
     }
   }
 }
 
+template <int L>
 __global__ void __launch_bounds__(256) reassemble_kernel(const __grid_constant__ CrtConst cc, const uint16_t *res,
                                                          int64_t Mp, int64_t plane, int64_t M, int64_t N,
                                                          const int *e_row, const int *e_col, double alpha,
                                                          double *C, int64_t ldc) {
-  reassemble_body(cc, res, Mp, plane, M, N, e_row, e_col, alpha, C, ldc, blockIdx.x, blockIdx.y, gridDim.y);
+  reassemble_body<L>(cc, res, Mp, plane, M, N, e_row, e_col, alpha, C, ldc, blockIdx.x, blockIdx.y, gridDim.y);
 }
 
 // ---------------------------------------------------------------- grouped (wave) kernels
@@ -485,8 +454,17 @@ __global__ void __launch_bounds__(256) reassemble_wave_kernel(const CrtJob *jobs
   if (b >= total) return;
   const CrtJob &J = jobs[find_job(jobs, n, b)];
   const int64_t lb = b - J.block_begin;
-  reassemble_body(J.cc, J.res, J.Mp, J.plane, J.M, J.N, J.e_row, J.e_col, J.alpha, J.C, J.ldc, lb % J.gx, lb / J.gx,
-                  J.N);
+  const CrtConst &cc = J.cc;
+  switch (cc.limbs) {
+#define UVT_CRT_CASE(L)                                                                                           \
+  case L:                                                                                                         \
+    reassemble_body<L>(cc, J.res, J.Mp, J.plane, J.M, J.N, J.e_row, J.e_col, J.alpha, J.C, J.ldc, lb % J.gx,      \
+                       lb / J.gx, J.N);                                                                           \
+    break;
+    UVT_CRT_CASE(2) UVT_CRT_CASE(3) UVT_CRT_CASE(4) UVT_CRT_CASE(5) UVT_CRT_CASE(6)
+#undef UVT_CRT_CASE
+    default: break;
+  }
 }
 
 dim3 flat_grid(int64_t total) {
@@ -519,23 +497,13 @@ Big big_div_small(const Big &a, uint64_t s, uint64_t *rem) {
   *rem = (uint64_t)r;
   return q;
 }
+double big_to_double(const Big &a) {
+  return (double)a.w[2] * 0x1p128 + (double)a.w[1] * 0x1p64 + (double)a.w[0];
+}
 double big_log2(const Big &a) {
   double v = (double)a.w[2] * 0x1p128 + (double)a.w[1] * 0x1p64 + (double)a.w[0];
   return std::log2(v);
 }
-int64_t inv_mod(int64_t a, int64_t m) {
-  int64_t g = m, x = 0, x1 = 1, a1 = a % m;
-  while (a1) {
-    int64_t q = g / a1, t = g - q * a1;
-    g = a1;
-    a1 = t;
-    t = x - q * x1;
-    x = x1;
-    x1 = t;
-  }
-  return ((x % m) + m) % m;
-}
-
 Big modulus_product(int n) {
   Big M;
   M.w[0] = 1;
@@ -581,34 +549,29 @@ int oz_residues(const OzOperand &op, const int *e, int bits, int l0, int l1, int
 }
 
 namespace {
-// CRT constants for the first n moduli: W_l = (M/m_l) * ((M/m_l)^-1 mod m_l).
+// CRT constants for the first n moduli: P_l = M/m_l, M, the limb count L
+// (smallest >= 2 with M < 2^(32L)) and the scales of the k estimate.
 CrtConst make_crt(const OzPlan &plan) {
   CrtConst cc;
   memset(&cc, 0, sizeof(cc));
   cc.n = plan.n_moduli;
   cc.bits = plan.bits;
   const Big M = modulus_product(plan.n_moduli);
+  auto limb = [](const Big &v, int k) { return (uint32_t)(v.w[k / 2] >> (32 * (k % 2))); };
+  int top = 0;
+  for (int k = 0; k < kLimbs; ++k) {
+    cc.Mw[k] = limb(M, k);
+    if (cc.Mw[k]) top = k;
+  }
+  cc.limbs = std::max(2, top + 1);
   for (int l = 0; l < plan.n_moduli; ++l) {
     uint64_t rem;
-    const Big Ml = big_div_small(M, (uint64_t)kModuli[l], &rem);
-    uint64_t mlm;
-    big_div_small(Ml, (uint64_t)kModuli[l], &mlm);
-    const int64_t inv = inv_mod((int64_t)mlm, kModuli[l]);
-    const Big W = big_mul_small(Ml, (uint64_t)inv);
-    for (int k = 0; k < kLimbs; ++k) cc.W[l][k] = (uint32_t)(W.w[k / 2] >> (32 * (k % 2)));
+    const Big Pl = big_div_small(M, (uint64_t)kModuli[l], &rem);
+    for (int k = 0; k < kLimbs; ++k) cc.P[l][k] = limb(Pl, k);
   }
-  uint64_t r2;
-  const Big half = big_div_small(M, 2, &r2);
-  int mt = 0;
-  for (int k = 0; k < kLimbs; ++k) {
-    cc.Mw[k] = (uint32_t)(M.w[k / 2] >> (32 * (k % 2)));
-    cc.halfM[k] = (uint32_t)(half.w[k / 2] >> (32 * (k % 2)));
-    if (cc.Mw[k]) mt = k;
-  }
-  cc.base = std::min(std::max(mt - 1, 0), kLimbs - 3);
-  double mf = 0.0;  // M / 2^(32 base)
-  for (int k = kLimbs - 1; k >= cc.base; --k) mf = mf * 4294967296.0 + (double)cc.Mw[k];
-  cc.inv_mf = (float)(1.0 / mf);
+  const double mf = big_to_double(M);
+  cc.c_hi = (float)(std::ldexp(1.0, 32 * (cc.limbs - 1)) / mf);
+  cc.c_lo = (float)(std::ldexp(1.0, 32 * (cc.limbs - 2)) / mf);
   return cc;
 }
 }  // namespace
@@ -698,8 +661,16 @@ int oz_reassemble(const OzPlan &plan, const uint16_t *res, const int *e_row, con
   const CrtConst cc = make_crt(plan);
   if (plan.M <= 0 || plan.N <= 0) return UVATRMM_OK;
   dim3 grid((unsigned)((plan.M + 256 * kCrtRows - 1) / (256 * kCrtRows)), (unsigned)std::min<int64_t>(plan.N, 65535));
-  reassemble_kernel<<<grid, 256, 0, st>>>(cc, res, plan.Mp, plan.Mp * plan.Np, plan.M, plan.N, e_row, e_col,
-                                           alpha, C, ldc);
+  switch (cc.limbs) {
+#define UVT_CRT_LAUNCH(L)                                                                                         \
+  case L:                                                                                                         \
+    reassemble_kernel<L><<<grid, 256, 0, st>>>(cc, res, plan.Mp, plan.Mp * plan.Np, plan.M, plan.N, e_row, e_col, \
+                                               alpha, C, ldc);                                                    \
+    break;
+    UVT_CRT_LAUNCH(2) UVT_CRT_LAUNCH(3) UVT_CRT_LAUNCH(4) UVT_CRT_LAUNCH(5) UVT_CRT_LAUNCH(6)
+#undef UVT_CRT_LAUNCH
+    default: return UVATRMM_EINVAL;
+  }
   return cudaGetLastError() == cudaSuccess ? UVATRMM_OK : UVATRMM_EDEVICE;
 }
 

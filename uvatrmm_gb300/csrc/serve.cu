@@ -295,6 +295,7 @@ int setup(uvatrmm_server_t s, Req &r) {
     L.Mp = pl.Mp; L.Np = pl.Np; L.Kp = pl.Kp; L.M = pl.M; L.N = pl.N; L.K = pl.K;
     L.l0 = 0;
     L.l1 = pl.n_moduli;
+    L.n_moduli = pl.n_moduli;
     L.tri_left = t.side == CblasLeft;
     L.tri_lower = (t.uplo == CblasLower) != (t.trans != 0);
     L.raster_group = 0;
