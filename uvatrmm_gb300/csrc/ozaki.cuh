@@ -81,7 +81,12 @@ struct OzPlan {
 };
 
 // Padded extents of the residue planes: the residue GEMM's CTA pairs cover
-// 256 rows (two 128-row tiles) x 256 columns, its K slabs are 64 wide.
+// 256 rows (two 128-row tiles) x 256 columns, its K slabs are 64 wide.  The
+// K range of a pair (triangular Lft) or of a column tile (triangular Rgt) is
+// set per block of kOzBlock rows of the triangular operand: [0, b + 256) when
+// its nonzeros lie at k <= p, [b, K) when at k >= p (b = the block's first
+// row); the slicing skips the residue tiles outside it.
+constexpr int kOzBlock = 256;
 inline int64_t oz_pad_rows(int64_t M) { return (M + 255) / 256 * 256; }
 inline int64_t oz_pad_cols(int64_t N) { return (N + 255) / 256 * 256; }
 

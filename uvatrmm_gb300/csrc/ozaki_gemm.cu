@@ -46,6 +46,7 @@ namespace {
 
 constexpr int BM = 128, BN = 256, BK = 64;
 constexpr int PAIR = 2;          // CTAs per cluster, stacked along M
+static_assert(PAIR * BM == kOzBlock && BN == kOzBlock, "the slicing skips tiles by this K-range geometry");
 constexpr int BH = BN / PAIR;    // rows of the B tile each CTA loads and multicasts
 constexpr uint16_t PAIR_MASK = (1u << PAIR) - 1;
 constexpr int STAGES = 4;

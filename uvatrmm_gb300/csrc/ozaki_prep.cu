@@ -39,6 +39,7 @@ __device__ __forceinline__ int exp_above(double v) {
 
 // Tiles of 32 (p) x 64 (k) per 256-thread block; grid.y splits K.
 constexpr int TP = 32, TK = 64;
+static_assert(kOzBlock % TP == 0 && kOzBlock % TK == 0, "a residue tile lies in one K-range block");
 
 // Rows [32 bx, 32 bx + 32) of the operand over k in [by * kpb, (by+1) * kpb):
 // the maximum exponent per row.  `direct`: this block covers all of K, so it
@@ -169,6 +170,13 @@ __device__ __forceinline__ void residue_body(const OzOperand &op, const int *e, 
   __shared__ double tile[TP][TK + 1];
   const int tid = threadIdx.x;
   const int64_t p0 = by * TP, k0 = bx * TK;
+  if (op.tri) {
+    // The residue GEMM never reads this tile when its K slab is outside the
+    // range of the kOzBlock-row block holding it (see kOzBlock).
+    const int64_t b = p0 / kOzBlock * kOzBlock;
+    const bool k_le_p = op.p_is_row == op.lower;  // nonzeros at k <= p
+    if (k_le_p ? k0 >= b + kOzBlock : k0 + TK <= b) return;
+  }
   // Load (coalesced along the contiguous dimension of X).
   for (int idx = tid; idx < TP * TK; idx += 256) {
     int pp, kk;
