@@ -93,18 +93,25 @@ __device__ __forceinline__ int find_problem(const OzGroupProb *probs, int nprob,
 }
 
 // Local pair tile t of problem p: modulus, tile coordinates and K slab range.
-__device__ __forceinline__ Tile decode(const OzGroupProb &p, int t) {
+__device__ __forceinline__ Tile decode(const OzGroupProb &p, int t, int nclusters) {
   Tile T;
   T.l = p.l0 + t / p.tiles_per_mod;
   int r = t % p.tiles_per_mod;
   const int tpm = p.tiles_m / PAIR;
   const int n_maj = p.tri_left ? tpm : p.tiles_n, n_min = p.tri_left ? p.tiles_n : tpm;
   // Raster: groups of `group` major tiles in longest-first order; inside a
-  // group the minor index is outer, so concurrent clusters share both panels.
+  // group the minor index is outer, so the clusters of one wave (tiles
+  // c + k * nclusters) form a group x (nclusters / group) block sharing both
+  // panels.  The major tile of a minor index is rotated by the wave, so a
+  // cluster cycles through the group's (triangle-shortened) major tiles
+  // instead of keeping the shortest or longest one and drifting out of step
+  // with the clusters it shares panels with.
   const int gspan = p.group * n_min;
   const int g = r / gspan, within = r % gspan;
   const int gsize = min(p.group, n_maj - g * p.group);
-  const int mi = within / gsize, rank = g * p.group + within % gsize;
+  const int mi = within / gsize;
+  const int per_wave = max(1, nclusters / gsize);  // minor tiles per wave
+  const int rank = g * p.group + (within % gsize + mi / per_wave) % gsize;
   const int ma = p.grows ? (n_maj - 1 - rank) : rank;
   T.tp = p.tri_left ? ma : mi;
   T.tj = p.tri_left ? mi : ma;
@@ -279,7 +286,7 @@ __global__ void __cluster_dims__(PAIR, 1, 1) __launch_bounds__(NUM_THREADS, 1)
           tmap_acquire(&P.tmB);
           cur = pi;
         }
-        const Tile T = decode(P, t - P.tile_begin + P.tile_offset);
+        const Tile T = decode(P, t - P.tile_begin + P.tile_offset, (int)cluster_count());
         const int ya = (int)((T.l - P.l0) * P.Mp + ((int64_t)T.tp * PAIR + rank) * BM);
         const int yb = (int)((T.l - P.l0) * P.Np + (int64_t)T.tj * BN + rank * BH);
         for (int ks = T.ks0; ks < T.ks1; ++ks) {
@@ -309,7 +316,7 @@ __global__ void __cluster_dims__(PAIR, 1, 1) __launch_bounds__(NUM_THREADS, 1)
       bool ok = true, any = false;
       for (int t = (int)cluster_index(); ok && t < p.total_tiles; t += (int)cluster_count()) {
         const OzGroupProb &P = probs[find_problem(probs, p.nprob, t)];
-        const Tile T = decode(P, t - P.tile_begin + P.tile_offset);
+        const Tile T = decode(P, t - P.tile_begin + P.tile_offset, (int)cluster_count());
         const int nslab = T.ks1 - T.ks0;
         const int nchunk = (nslab + CHUNK_SLABS - 1) / CHUNK_SLABS;
         for (int c = 0; ok && c < nchunk; ++c, ++gc) {
@@ -358,7 +365,7 @@ __global__ void __cluster_dims__(PAIR, 1, 1) __launch_bounds__(NUM_THREADS, 1)
     bool ok = true;
     for (int t = (int)cluster_index(); ok && t < p.total_tiles; t += (int)cluster_count()) {
       const OzGroupProb &P = probs[find_problem(probs, p.nprob, t)];
-      const Tile T = decode(P, t - P.tile_begin + P.tile_offset);
+      const Tile T = decode(P, t - P.tile_begin + P.tile_offset, (int)cluster_count());
       const int nslab = T.ks1 - T.ks0;
       const int nchunk = (nslab + CHUNK_SLABS - 1) / CHUNK_SLABS;
       const float m = p.mod_f[T.l], inv = p.inv_f[T.l], cu = p.u_f[P.nmod][T.l];
@@ -497,7 +504,7 @@ int oz_group_prob(const OzGemmLaunch &L, OzGroupProb *out, const char **why) {
   out->tiles_n = (int)(L.Np / BN);
   out->tiles_per_mod = (out->tiles_m / PAIR) * out->tiles_n;
   out->tile_count = out->tiles_per_mod * nmod;
-  out->group = L.raster_group > 0 ? L.raster_group : 2;
+  out->group = L.raster_group > 0 ? L.raster_group : 4;
   out->res = L.res;
   out->plane = L.Mp * L.Np;
   out->nmod = L.n_moduli;
