@@ -662,6 +662,7 @@ def run_ozaki(args, h, dev, stream, rank, plain_tflops):
     h.gen_uniform(2, 1, m, n, dB0, 1, m, spread=20)
     h.sync()
     h.set_option("stage_timing", 1)
+    h.set_option("ozaki_raster", args.ozaki_raster)
     moduli, bits = u.ozaki_plan(m)
 
     def step(mo=0, want_err=False):
@@ -704,6 +705,7 @@ def run_ozaki(args, h, dev, stream, rank, plain_tflops):
             sweep.append({"moduli": mo, "bits": b, "rel_fro_err_vs_dd_oracle": float(
                 np.linalg.norm(got - ref) / np.linalg.norm(ref)), "rel_fro_err_vs_plain_fp64_gpu": est})
     h.set_option("stage_timing", 0)
+    h.set_option("ozaki_raster", 0)
     del dA, dB0, dB
     torch.cuda.empty_cache()
     auto = next((s for s in sweep if s["moduli"] == moduli), None)
@@ -739,6 +741,8 @@ def main():
     ap.add_argument("--no-ozaki", action="store_true")
     ap.add_argument("--ozaki-n", type=int, default=32768)
     ap.add_argument("--ozaki-steps", type=int, default=3)
+    ap.add_argument("--ozaki-raster", type=int, default=0,
+                    help="residue-GEMM raster group (pair rows per group; 0 = library default)")
     ap.add_argument("--no-variants", dest="variants", action="store_false")
     ap.add_argument("--big-n", type=int, default=32768)
     ap.add_argument("--next-n", type=int, default=8192)
