@@ -53,7 +53,12 @@ constexpr int STAGES = 4;
 constexpr int CHUNK_SLABS = 8;  // K chunk of 512 between modular folds
 constexpr uint32_t A_BYTES = BM * BK * 2, B_BYTES = BN * BK * 2, BH_BYTES = BH * BK * 2;
 constexpr uint32_t STAGE_BYTES = A_BYTES + B_BYTES;
-constexpr int NUM_THREADS = 192;
+// Warp 0: TMA producer; warp 1: MMA issuer; warps 2..9: epilogue, two warps
+// per TMEM lane quarter (warp & 3), each taking half of the 256 columns, so a
+// tile's last-chunk epilogue stays within one chunk of MMAs.
+constexpr int EPI_WARPS = 8;
+constexpr int CB_PER_WARP = BN / 32 / (EPI_WARPS / 4);  // 32-column blocks per epilogue warp
+constexpr int NUM_THREADS = 32 * (2 + EPI_WARPS);
 constexpr uint32_t TMEM_COLS = 2 * BN;  // two fp32 accumulators of 256 columns
 // Low bytes of a tile's second-to-last chunk residues, [column word][row] (32 KB).
 constexpr uint32_t R1_BYTES = BM * BN;
@@ -253,7 +258,7 @@ __global__ void __cluster_dims__(PAIR, 1, 1) __launch_bounds__(NUM_THREADS, 1)
     }
     for (int b = 0; b < 2; ++b) {
       mbar_init(&cdone[b], 1);
-      mbar_init(&afree[b], 4);
+      mbar_init(&afree[b], EPI_WARPS);
     }
     mbar_init(drain, 1);
     fence_barrier_init();
@@ -359,6 +364,7 @@ __global__ void __cluster_dims__(PAIR, 1, 1) __launch_bounds__(NUM_THREADS, 1)
   } else {
     // ------------------------------------------------------------ epilogue
     const int quad = warp & 3;
+    const int cb0 = ((warp - 2) >> 2) * CB_PER_WARP;  // this warp's first 32-column block
     const int row = quad * 32 + lane;
     const uint32_t lane_base = tmem_base + ((uint32_t)(quad * 32) << 16);
     uint32_t gc = 0;
@@ -372,7 +378,7 @@ __global__ void __cluster_dims__(PAIR, 1, 1) __launch_bounds__(NUM_THREADS, 1)
       // This thread's row of the tile's residue output (column stride Mp).
       uint16_t *out = P.res + (int64_t)T.l * P.plane + ((int64_t)T.tp * PAIR + rank) * BM + row;
       uint32_t *r1 = r1s + row;  // this row's words of r1s, stride BM (each thread touches only its own)
-      uint32_t hib[BN / 32];     // ninth bits of the second-to-last chunk's residues
+      uint32_t hib[CB_PER_WARP];  // ninth bits of the second-to-last chunk's residues
       for (int c = 0; c < nchunk; ++c, ++gc) {
         const uint32_t b = gc & 1u, u = gc >> 1;
         if (!mbar_wait_bounded(&cdone[b], u & 1u)) {
@@ -385,7 +391,7 @@ __global__ void __cluster_dims__(PAIR, 1, 1) __launch_bounds__(NUM_THREADS, 1)
         if (c + 2 < nchunk) {
           // Fold: acc := acc - m * rint(acc / m), exact in fp32.
 #pragma unroll 1
-          for (int cb = 0; cb < BN / 32; ++cb) {
+          for (int cb = cb0; cb < cb0 + CB_PER_WARP; ++cb) {
             uint32_t v[32];
             tmem_ld32(tb + (uint32_t)(cb * 32), v);
             tmem_wait_ld();
@@ -400,7 +406,7 @@ __global__ void __cluster_dims__(PAIR, 1, 1) __launch_bounds__(NUM_THREADS, 1)
         } else if (c + 2 == nchunk) {
           // Second-to-last chunk: its residues move aside, the buffer is freed now.
 #pragma unroll 1
-          for (int cb = 0; cb < BN / 32; ++cb) {
+          for (int cb = cb0; cb < cb0 + CB_PER_WARP; ++cb) {
             uint32_t v[32];
             tmem_ld32(tb + (uint32_t)(cb * 32), v);
             tmem_wait_ld();
@@ -416,7 +422,7 @@ __global__ void __cluster_dims__(PAIR, 1, 1) __launch_bounds__(NUM_THREADS, 1)
               }
               r1[(cb * 8 + q) * BM] = w;
             }
-            hib[cb] = hi;
+            hib[cb - cb0] = hi;
           }
         } else {
           // Last chunk: with v this chunk's sum and p the parked residue, the
@@ -426,12 +432,12 @@ __global__ void __cluster_dims__(PAIR, 1, 1) __launch_bounds__(NUM_THREADS, 1)
           // may come out one low, which the single correction handles.
           const bool two = nchunk >= 2;
 #pragma unroll 1
-          for (int cb = 0; cb < BN / 32; ++cb) {
+          for (int cb = cb0; cb < cb0 + CB_PER_WARP; ++cb) {
             uint32_t v[32];
             tmem_ld32(tb + (uint32_t)(cb * 32), v);
             tmem_wait_ld();
             const int64_t j0 = (int64_t)T.tj * BN + cb * 32;
-            const uint32_t hi = two ? hib[cb] : 0u;
+            const uint32_t hi = two ? hib[cb - cb0] : 0u;
 #pragma unroll
             for (int q = 0; q < 8; ++q) {
               const uint32_t w = two ? r1[(cb * 8 + q) * BM] : 0u;
