@@ -93,7 +93,7 @@ typedef enum {
   UVATRMM_OPT_STAGE_TIMING = 6,     /* 1: time the stages of each Ozaki call (uvatrmm_stage_times) */
   UVATRMM_OPT_AUTOTUNE = 7,         /* 1 (default): measure untuned shape buckets; 0: defaults only */
   UVATRMM_OPT_OZAKI_RASTER = 8      /* Ozaki residue GEMM of single calls: major tiles per raster
-                                       group (0 = default 4, else 1..64) */
+                                       group (0 = default: 4 when m, n >= 16384, else 2; or 1..64) */
 } uvatrmm_option;
 typedef enum { UVATRMM_ENGINE_DFMA = 0, UVATRMM_ENGINE_DMMA = 1 } uvatrmm_engine;
 /* DYNAMIC: persistent CTAs pull tiles in longest-first order.

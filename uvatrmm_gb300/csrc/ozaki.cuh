@@ -140,7 +140,7 @@ struct OzGemmLaunch {
   int l0, l1;
   int n_moduli = 0;  // moduli of the CRT set (sets u_l of the stored residues)
   bool tri_left, tri_lower;
-  int raster_group = 0;          // major tiles per raster group (0 = default, 4)
+  int raster_group = 0;          // major tiles per raster group (0 = default: 4 from m, n >= 16384, else 2)
   OzGroupProb *desc = nullptr;   // device slot for the descriptor (single launches)
   int *status;
   int num_sms;

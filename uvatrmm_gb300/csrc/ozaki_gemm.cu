@@ -510,7 +510,10 @@ int oz_group_prob(const OzGemmLaunch &L, OzGroupProb *out, const char **why) {
   out->tiles_n = (int)(L.Np / BN);
   out->tiles_per_mod = (out->tiles_m / PAIR) * out->tiles_n;
   out->tile_count = out->tiles_per_mod * nmod;
-  out->group = L.raster_group > 0 ? L.raster_group : 4;
+  // Default raster group (measured at m = n = 1024 .. 32768): 4 pair rows once
+  // both tile counts reach 64 (m, n >= 16384), 2 below.
+  const bool big = out->tiles_m / PAIR >= 64 && out->tiles_n >= 64;
+  out->group = L.raster_group > 0 ? L.raster_group : (big ? 4 : 2);
   out->res = L.res;
   out->plane = L.Mp * L.Np;
   out->nmod = L.n_moduli;
