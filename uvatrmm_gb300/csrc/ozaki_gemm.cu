@@ -11,8 +11,8 @@
 // at most 181 in magnitude (moduli up to 363) and a folded value at most a
 // few units past m/2, so every value the accumulator ever holds is an
 // integer below 512 * 181^2 + 184 < 2^24 and fp32 accumulation is exact.
-// The last two chunks are combined and the tile's residues (0 <= r < m_l)
-// are written as 16-bit words.
+// The last two chunks are combined and the tile's residues r are written as
+// the 16-bit words u_l r mod m_l (u_l = (M/m_l)^-1 mod m_l, for the CRT).
 //
 // CTA pairs.  The kernel runs in clusters of two CTAs stacked along M: the
 // pair computes a 256 x 256 block (rows 2*tp*128 + rank*128 for each CTA)
@@ -29,9 +29,11 @@
 // columns) and its buffer released at once, so the next tile's first chunk
 // runs while the last chunk is combined and stored.
 //
-// Warp roles (192 threads, one CTA per SM): warp 0 TMA producer, warp 1 TMEM
-// owner + MMA issuer, warps 2-5 epilogue (each bound to its TMEM lane
-// quadrant, warp % 4).  All mbarrier waits are bounded; on expiry the kernel
+// Warp roles (320 threads, one CTA per SM): warp 0 TMA producer, warp 1 TMEM
+// owner + MMA issuer, warps 2-9 epilogue (each bound to its TMEM lane
+// quadrant, warp % 4, and to half of the columns).  Tiles go to clusters
+// round-robin in a raster of pair-row groups (see decode()).  All mbarrier
+// waits are bounded; on expiry the kernel
 // records KERR_WAIT_TIMEOUT, drains its copies and MMAs, frees TMEM and exits
 // (after the pair's closing cluster barrier).
 #include <algorithm>
