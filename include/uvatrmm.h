@@ -358,6 +358,14 @@ UVATRMM_API int uvatrmm_probe_fp64_peak(uvatrmm_handle_t handle, int engine, dou
 UVATRMM_API int uvatrmm_device_alloc(size_t bytes, void **ptr);
 UVATRMM_API int uvatrmm_device_free(void *ptr);
 UVATRMM_API int uvatrmm_copy(uvatrmm_handle_t handle, void *dst, const void *src, size_t bytes, int kind);
+/* Page-locked host memory for the operands of the host entry points
+ * (uvatrmm_dtrmm, cblas_dtrmm, ...): zeroed, aligned to the transparent-huge-
+ * page size and backed by huge pages where the kernel grants them.  On GB300
+ * hosts such buffers keep their full copy rate (2 GiB in ~10 ms) where
+ * cudaHostAlloc'd or malloc'd buffers slow down as they age.  Free with
+ * uvatrmm_host_free (NULL is accepted; other pointers give UVATRMM_EINVAL). */
+UVATRMM_API int uvatrmm_host_alloc(size_t bytes, void **ptr);
+UVATRMM_API int uvatrmm_host_free(void *ptr);
 
 /* ---------------------------------------------------------------- errors */
 UVATRMM_API const char *uvatrmm_last_error(void);

@@ -247,6 +247,21 @@ class Server:
             pass
 
 
+def host_empty(count: int, dtype="float64"):
+    """A numpy array of `count` elements in page-locked, huge-page-backed host
+    memory from uvatrmm_host_alloc (zeroed); freed when the array is collected.
+    Operands of the host entry points keep their full copy rate in it."""
+    import weakref
+
+    import numpy as np
+    dt = np.dtype(dtype)
+    p = C.c_void_p()
+    check(lib().uvatrmm_host_alloc(max(1, count) * dt.itemsize, C.byref(p)))
+    buf = (C.c_char * (max(1, count) * dt.itemsize)).from_address(p.value)
+    weakref.finalize(buf, lib().uvatrmm_host_free, p.value)
+    return np.frombuffer(buf, dtype=dt, count=count)
+
+
 def tune(handle: "Handle", tier: int, side: int, m: int, n: int) -> int:
     c = C.c_int()
     check(lib().uvatrmm_tune(handle.h, tier, side, m, n, C.byref(c)))

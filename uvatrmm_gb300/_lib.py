@@ -44,6 +44,8 @@ SIGNATURES = {
     "uvatrmm_device_alloc": (i32, [C.c_size_t, C.POINTER(vp)]),
     "uvatrmm_device_free": (i32, [vp]),
     "uvatrmm_copy": (i32, [vp, vp, vp, C.c_size_t, i32]),
+    "uvatrmm_host_alloc": (i32, [C.c_size_t, C.POINTER(vp)]),
+    "uvatrmm_host_free": (i32, [vp]),
     "uvatrmm_last_error": (C.c_char_p, []),
     "uvatrmm_last_status": (i32, []),
     "uvatrmm_version": (C.c_char_p, []),
