@@ -92,8 +92,10 @@ typedef enum {
   UVATRMM_OPT_OZAKI_SCRATCH_MB = 5, /* Ozaki residue-plane budget per pass, MiB (default 49152) */
   UVATRMM_OPT_STAGE_TIMING = 6,     /* 1: time the stages of each Ozaki call (uvatrmm_stage_times) */
   UVATRMM_OPT_AUTOTUNE = 7,         /* 1 (default): measure untuned shape buckets; 0: defaults only */
-  UVATRMM_OPT_OZAKI_RASTER = 8      /* Ozaki residue GEMM of single calls: major tiles per raster
+  UVATRMM_OPT_OZAKI_RASTER = 8,     /* Ozaki residue GEMM of single calls: major tiles per raster
                                        group (0 = default: 4 when m, n >= 16384, else 2; or 1..64) */
+  UVATRMM_OPT_HOST_STAGE_KB = 9     /* chunk of the host staging used for host operands outside
+                                       uvatrmm_host_alloc memory, KiB (0 = default 262144; >= 64) */
 } uvatrmm_option;
 typedef enum { UVATRMM_ENGINE_DFMA = 0, UVATRMM_ENGINE_DMMA = 1 } uvatrmm_engine;
 /* DYNAMIC: persistent CTAs pull tiles in longest-first order.
@@ -113,6 +115,16 @@ UVATRMM_API int uvatrmm_dtrmm(uvatrmm_handle_t handle, int layout, int side, int
                               int64_t m, int64_t n, double alpha, const double *A, int64_t lda, double *B,
                               int64_t ldb);
 
+/* Asynchronous uvatrmm_dtrmm for pipelines: enqueues the copies of A and B
+ * to the device, the product and the copy of the result into B on the
+ * handle's stream, and returns.  A and B must lie in uvatrmm_host_alloc
+ * memory (else UVATRMM_EINVAL) and stay untouched until uvatrmm_sync(handle),
+ * which waits and reports the kernel status.  Calls on one handle run in
+ * order; calls on two handles overlap one problem's copies with the other's
+ * product. */
+UVATRMM_API int uvatrmm_dtrmm_async(uvatrmm_handle_t handle, int layout, int side, int uplo, int transa, int diag,
+                                    int64_t m, int64_t n, double alpha, const double *A, int64_t lda, double *B,
+                                    int64_t ldb);
 /* Device buffers, in place on dB, ordered on the handle's stream (returns
  * once the work is enqueued; errors from kernels surface at the next
  * synchronising call or uvatrmm_sync). */

@@ -62,7 +62,8 @@ class Handle:
 
     def set_option(self, name: str, value: int) -> None:
         key = {"engine": OPT_ENGINE, "schedule": OPT_SCHEDULE, "shape": OPT_SHAPE, "tile": OPT_TILE,
-               "ozaki_scratch_mb": 5, "stage_timing": 6, "autotune": 7, "ozaki_raster": 8}[name]
+               "ozaki_scratch_mb": 5, "stage_timing": 6, "autotune": 7, "ozaki_raster": 8,
+               "host_stage_kb": 9}[name]
         check(lib().uvatrmm_set_option(self.h, key, int(value)))
 
     def stage_times(self):
@@ -76,6 +77,12 @@ class Handle:
         """Host buffers (numpy float64), in place on B."""
         check(lib().uvatrmm_dtrmm(self.h, layout, side, uplo, transa, diag, m, n, alpha,
                                   _ptr(A), lda, _ptr(B), ldb))
+
+    def dtrmm_async(self, layout, side, uplo, transa, diag, m, n, alpha, A, lda, B, ldb) -> None:
+        """Host buffers from host_empty(), in place on B; enqueued on the
+        handle's stream, complete after sync()."""
+        check(lib().uvatrmm_dtrmm_async(self.h, layout, side, uplo, transa, diag, m, n, alpha,
+                                        _ptr(A), lda, _ptr(B), ldb))
 
     def dtrmm_device(self, layout, side, uplo, transa, diag, m, n, alpha, dA, lda, dB, ldb) -> None:
         """Device buffers (torch float64 CUDA tensors), in place on dB."""

@@ -25,6 +25,7 @@ SIGNATURES = {
     "uvatrmm_set_stream": (i32, [vp, vp]),
     "uvatrmm_set_option": (i32, [vp, i32, i32]),
     "uvatrmm_dtrmm": (i32, [vp, i32, i32, i32, i32, i32, i64, i64, dbl, vp, i64, vp, i64]),
+    "uvatrmm_dtrmm_async": (i32, [vp, i32, i32, i32, i32, i32, i64, i64, dbl, vp, i64, vp, i64]),
     "uvatrmm_dtrmm_device": (i32, [vp, i32, i32, i32, i32, i32, i64, i64, dbl, vp, i64, vp, i64]),
     "uvatrmm_dtrmm_device_oop": (i32, [vp, i32, i32, i32, i32, i32, i64, i64, dbl, vp, i64, vp, i64, vp, i64]),
     "uvatrmm_sync": (i32, [vp]),

@@ -124,14 +124,6 @@ namespace {
 
 bool tma_ok(const void *p, int64_t ld) { return (reinterpret_cast<uintptr_t>(p) % 16 == 0) && (ld % 2 == 0); }
 
-// 2-D copy; one linear copy when both sides are contiguous.
-cudaError_t copy2d(void *dst, size_t dpitch, const void *src, size_t spitch, size_t width, size_t height,
-                   cudaMemcpyKind kind, cudaStream_t st) {
-  if (width == 0 || height == 0) return cudaSuccess;
-  if (dpitch == width && spitch == width) return cudaMemcpyAsync(dst, src, width * height, kind, st);
-  return cudaMemcpy2DAsync(dst, dpitch, src, spitch, width, height, kind, st);
-}
-
 // Launches C := alpha*op(A)*B or alpha*B*op(A) on device buffers, all
 // column-major; A and B must satisfy tma_ok.
 int run_fp64(uvatrmm_handle_t h, const Trmm &t, const double *A, int64_t lda, const double *B, int64_t ldb,
@@ -224,6 +216,45 @@ int device_trmm(uvatrmm_handle_t h, int layout, int side, int uplo, int transa, 
   return rc == UVATRMM_OK ? ok() : rc;
 }
 
+// The host-pointer TRMM: A and B copied in, C := alpha op(A) B (or B op(A))
+// computed out of place, C copied back into B.  `async`: A and B must lie in
+// uvatrmm_host_alloc memory, everything is enqueued on the handle's stream
+// and the status is collected by uvatrmm_sync.
+int host_trmm(uvatrmm_handle_t h, int layout, int side, int uplo, int transa, int diag, int64_t m, int64_t n,
+              double alpha, const double *A, int64_t lda, double *B, int64_t ldb, bool async) {
+  if (int bad = check_args(layout, side, uplo, transa, diag, m, n, lda, ldb))
+    return fail(UVATRMM_EINVAL, "parameter " + std::to_string(bad) + " had an illegal value");
+  Trmm t = normalise(layout, side, uplo, transa, diag, m, n, alpha);
+  if (t.m == 0 || t.n == 0) return ok();
+  const int64_t ka = t.side == CblasLeft ? t.m : t.n;
+  if (async && (!host_alloc_contains(A, (size_t)(lda * (ka - 1) + ka) * 8) ||
+                !host_alloc_contains(B, (size_t)(ldb * (t.n - 1) + t.m) * 8)))
+    return fail(UVATRMM_EINVAL, "asynchronous host operands must lie in uvatrmm_host_alloc memory");
+  if (alpha == 0.0) {
+    if (async) {
+      cudaError_t e = cudaStreamSynchronize(h->stream);  // earlier calls may still write B
+      if (e != cudaSuccess) return cuda_fail(e, "stream synchronise");
+    }
+    for (int64_t j = 0; j < t.n; ++j) memset(B + j * ldb, 0, (size_t)t.m * 8);
+    return ok();
+  }
+  const int64_t la = round_up(ka, 16), lb = round_up(t.m, 16);
+  double *dA = static_cast<double *>(workspace(h, 0, (size_t)la * ka * 8));
+  double *dB = static_cast<double *>(workspace(h, 1, (size_t)lb * t.n * 8));
+  double *dC = static_cast<double *>(workspace(h, 2, (size_t)lb * t.n * 8));
+  if (!dA || !dB || !dC) return tl_status;
+  cudaError_t e = host_copy2d(h, dA, la * 8, A, lda * 8, ka * 8, ka, cudaMemcpyHostToDevice);
+  if (e == cudaSuccess) e = host_copy2d(h, dB, lb * 8, B, ldb * 8, t.m * 8, t.n, cudaMemcpyHostToDevice);
+  if (e != cudaSuccess) return cuda_fail(e, "host to device copy");
+  int rc = run_fp64(h, t, dA, la, dB, lb, dC, lb, h->schedule, h->shape);
+  if (rc != UVATRMM_OK) return rc;
+  e = host_copy2d(h, B, ldb * 8, dC, lb * 8, t.m * 8, t.n, cudaMemcpyDeviceToHost);
+  if (e != cudaSuccess) return cuda_fail(e, "device to host copy");
+  if (async) return ok();
+  rc = collect_status(h);
+  return rc == UVATRMM_OK ? ok() : rc;
+}
+
 }  // namespace uvt
 
 using namespace uvt;
@@ -268,6 +299,7 @@ UVATRMM_API int uvatrmm_destroy(uvatrmm_handle_t h) {
   if (h->dctl) cudaFree(h->dctl);
   if (h->ev0) cudaEventDestroy(h->ev0);
   if (h->ev1) cudaEventDestroy(h->ev1);
+  release_host_staging(h);
   for (auto &ev : h->sev)
     if (ev) cudaEventDestroy(ev);
   for (auto &d : tl_default)
@@ -308,6 +340,10 @@ UVATRMM_API int uvatrmm_set_option(uvatrmm_handle_t h, int option, int value) {
     case UVATRMM_OPT_OZAKI_RASTER:
       if (value < 0 || value > 64) break;
       h->oz_raster = value;
+      return ok();
+    case UVATRMM_OPT_HOST_STAGE_KB:
+      if (value != 0 && value < 64) break;
+      h->hstage_bytes = (size_t)(value ? value : 262144) << 10;
       return ok();
     case UVATRMM_OPT_AUTOTUNE:
       if (value != 0 && value != 1) break;
@@ -354,29 +390,15 @@ UVATRMM_API int uvatrmm_dtrmm(uvatrmm_handle_t h, int layout, int side, int uplo
                               int64_t n, double alpha, const double *A, int64_t lda, double *B, int64_t ldb) {
   if (!(h = resolve(h))) return tl_status;
   std::lock_guard<std::mutex> g(h->mu);
-  if (int bad = check_args(layout, side, uplo, transa, diag, m, n, lda, ldb))
-    return fail(UVATRMM_EINVAL, "parameter " + std::to_string(bad) + " had an illegal value");
-  Trmm t = normalise(layout, side, uplo, transa, diag, m, n, alpha);
-  if (t.m == 0 || t.n == 0) return ok();
-  if (alpha == 0.0) {
-    for (int64_t j = 0; j < t.n; ++j) memset(B + j * ldb, 0, (size_t)t.m * 8);
-    return ok();
-  }
-  const int64_t ka = t.side == CblasLeft ? t.m : t.n;
-  const int64_t la = round_up(ka, 16), lb = round_up(t.m, 16);
-  double *dA = static_cast<double *>(workspace(h, 0, (size_t)la * ka * 8));
-  double *dB = static_cast<double *>(workspace(h, 1, (size_t)lb * t.n * 8));
-  double *dC = static_cast<double *>(workspace(h, 2, (size_t)lb * t.n * 8));
-  if (!dA || !dB || !dC) return tl_status;
-  cudaError_t e = copy2d(dA, la * 8, A, lda * 8, ka * 8, ka, cudaMemcpyHostToDevice, h->stream);
-  if (e == cudaSuccess) e = copy2d(dB, lb * 8, B, ldb * 8, t.m * 8, t.n, cudaMemcpyHostToDevice, h->stream);
-  if (e != cudaSuccess) return cuda_fail(e, "host to device copy");
-  int rc = run_fp64(h, t, dA, la, dB, lb, dC, lb, h->schedule, h->shape);
-  if (rc != UVATRMM_OK) return rc;
-  e = copy2d(B, ldb * 8, dC, lb * 8, t.m * 8, t.n, cudaMemcpyDeviceToHost, h->stream);
-  if (e != cudaSuccess) return cuda_fail(e, "device to host copy");
-  rc = collect_status(h);
-  return rc == UVATRMM_OK ? ok() : rc;
+  return host_trmm(h, layout, side, uplo, transa, diag, m, n, alpha, A, lda, B, ldb, false);
+}
+
+UVATRMM_API int uvatrmm_dtrmm_async(uvatrmm_handle_t h, int layout, int side, int uplo, int transa, int diag,
+                                    int64_t m, int64_t n, double alpha, const double *A, int64_t lda, double *B,
+                                    int64_t ldb) {
+  if (!(h = resolve(h))) return tl_status;
+  std::lock_guard<std::mutex> g(h->mu);
+  return host_trmm(h, layout, side, uplo, transa, diag, m, n, alpha, A, lda, B, ldb, true);
 }
 
 UVATRMM_API void cblas_dtrmm(CBLAS_LAYOUT layout, CBLAS_SIDE side, CBLAS_UPLO uplo, CBLAS_TRANSPOSE transa,

@@ -37,6 +37,12 @@ struct uvatrmm_handle_st {
   cudaEvent_t sev[kStageEvents] = {};
   int n_sev = 0;
   int sev_kind[kStageEvents] = {};  // stage the interval ending at this event belongs to
+  // Host staging for host operands outside uvatrmm_host_alloc memory: two
+  // page-locked huge-page buffers used alternately (host_mem.cu).
+  size_t hstage_bytes = (size_t)256 << 20;  // chunk size (UVATRMM_OPT_HOST_STAGE_KB)
+  void *hstage[2] = {};
+  size_t hstage_cap = 0;
+  cudaEvent_t hstage_ev[2] = {};
   std::mutex mu;
 };
 
@@ -53,6 +59,18 @@ uvatrmm_handle_t resolve(uvatrmm_handle_t h);
 
 // Ensures workspace slot `slot` holds at least `bytes`; returns its pointer or nullptr.
 void *workspace(uvatrmm_handle_t h, int slot, size_t bytes);
+
+// Host <-> device 2-D copy (`width` bytes x `height` lines) for the host
+// entry points, ordered on h->stream.  Host memory from uvatrmm_host_alloc
+// is copied directly; other host memory goes through the handle's staging
+// buffers, packed by several CPU threads while the previous chunk's DMA
+// runs.  A device-to-host copy has landed in `dst` when this returns.
+cudaError_t host_copy2d(uvatrmm_handle_t h, void *dst, size_t dpitch, const void *src, size_t spitch, size_t width,
+                        size_t height, cudaMemcpyKind kind);
+// True when [p, p + bytes) lies inside one uvatrmm_host_alloc region.
+bool host_alloc_contains(const void *p, size_t bytes);
+// Frees the handle's staging buffers and events.
+void release_host_staging(uvatrmm_handle_t h);
 
 // Reads and clears the kernel status word (synchronising the stream).
 int collect_status(uvatrmm_handle_t h);

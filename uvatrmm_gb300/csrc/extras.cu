@@ -212,15 +212,15 @@ UVATRMM_API int uvatrmm_dgemm(uvatrmm_handle_t h, int layout, int transa, int tr
   double *dC = static_cast<double *>(workspace(h, 2, (size_t)lc * ccn * 8 + 16));
   if (!dA || !dB || !dC) return uvatrmm_last_status();
   cudaError_t e = cudaSuccess;
-  if (ar && acn) e = cudaMemcpy2DAsync(dA, la * 8, A, lda * 8, ar * 8, acn, cudaMemcpyHostToDevice, h->stream);
+  if (ar && acn) e = host_copy2d(h, dA, la * 8, A, lda * 8, ar * 8, acn, cudaMemcpyHostToDevice);
   if (e == cudaSuccess && br && bcn)
-    e = cudaMemcpy2DAsync(dB, lb * 8, B, ldb * 8, br * 8, bcn, cudaMemcpyHostToDevice, h->stream);
+    e = host_copy2d(h, dB, lb * 8, B, ldb * 8, br * 8, bcn, cudaMemcpyHostToDevice);
   if (e == cudaSuccess && beta != 0.0)
-    e = cudaMemcpy2DAsync(dC, lc * 8, C, ldc * 8, cr * 8, ccn, cudaMemcpyHostToDevice, h->stream);
+    e = host_copy2d(h, dC, lc * 8, C, ldc * 8, cr * 8, ccn, cudaMemcpyHostToDevice);
   if (e != cudaSuccess) return cuda_fail(e, "host to device copy");
   int rc = device_gemm(h, layout, transa, transb, m, n, k, alpha, dA, la, dB, lb, beta, dC, lc);
   if (rc != UVATRMM_OK) return rc;
-  e = cudaMemcpy2DAsync(C, ldc * 8, dC, lc * 8, cr * 8, ccn, cudaMemcpyDeviceToHost, h->stream);
+  e = host_copy2d(h, C, ldc * 8, dC, lc * 8, cr * 8, ccn, cudaMemcpyDeviceToHost);
   if (e != cudaSuccess) return cuda_fail(e, "device to host copy");
   rc = collect_status(h);
   return rc == UVATRMM_OK ? ok() : rc;

@@ -9,15 +9,23 @@
 // huge pages (MADV_HUGEPAGE), touches it and page-locks it with
 // cudaHostRegister.  Where the kernel offers no huge pages the memory is
 // still page-locked and usable.
+//
+// The host entry points copy operands in such memory directly; other host
+// buffers (malloc'd, as the reference's, or page-locked elsewhere) are packed
+// into two staging buffers of this kind by several CPU threads, each chunk's
+// DMA overlapping the packing of the next (host_copy2d).
 #include <sys/mman.h>
 #include <unistd.h>
 
+#include <algorithm>
 #include <cstdint>
 #include <cstdio>
 #include <cstring>
 #include <map>
 #include <mutex>
 #include <string>
+#include <thread>
+#include <vector>
 
 #include "api_internal.h"
 
@@ -43,16 +51,17 @@ size_t huge_page_bytes() {
   return hp;
 }
 
-}  // namespace
-}  // namespace uvt
+// True when [p, p + bytes) lies inside one uvatrmm_host_alloc region.
+bool in_host_alloc(const void *p, size_t bytes) {
+  std::lock_guard<std::mutex> g(g_host_mu);
+  auto it = g_host_maps.upper_bound(const_cast<void *>(p));
+  if (it == g_host_maps.begin()) return false;
+  --it;
+  const uintptr_t base = reinterpret_cast<uintptr_t>(it->first), a = reinterpret_cast<uintptr_t>(p);
+  return a >= base && a + bytes <= base + it->second;
+}
 
-using namespace uvt;
-
-extern "C" {
-
-UVATRMM_API int uvatrmm_host_alloc(size_t bytes, void **ptr) {
-  if (!ptr) return fail(UVATRMM_EINVAL, "ptr is NULL");
-  *ptr = nullptr;
+int map_region(size_t bytes, void **out, size_t *len_out) {
   const size_t hp = huge_page_bytes();
   const size_t len = ((bytes ? bytes : 1) + hp - 1) / hp * hp;
   if (len < bytes) return fail(UVATRMM_EINVAL, "size overflows");
@@ -61,7 +70,7 @@ UVATRMM_API int uvatrmm_host_alloc(size_t bytes, void **ptr) {
   if (raw == MAP_FAILED) return fail(UVATRMM_ENOMEM, "mmap of " + std::to_string(len + hp) + " bytes failed");
   const uintptr_t a = reinterpret_cast<uintptr_t>(raw), b = (a + hp - 1) / hp * hp;
   if (b > a) munmap(raw, b - a);
-  if (b + len < a + len + hp) munmap(reinterpret_cast<void *>(b + len), a + len + hp - (b + len));
+  munmap(reinterpret_cast<void *>(b + len), a + hp - b);
   void *p = reinterpret_cast<void *>(b);
   madvise(p, len, MADV_HUGEPAGE);  // advisory: ignored where huge pages are off
   memset(p, 0, len);               // fault the pages in (as huge pages where granted)
@@ -74,8 +83,135 @@ UVATRMM_API int uvatrmm_host_alloc(size_t bytes, void **ptr) {
     std::lock_guard<std::mutex> g(g_host_mu);
     g_host_maps[p] = len;
   }
-  *ptr = p;
-  return ok();
+  *out = p;
+  *len_out = len;
+  return UVATRMM_OK;
+}
+
+// Copies `lines` lines of `width` bytes with up to 16 threads.
+void par_copy(void *dst, size_t dpitch, const void *src, size_t spitch, size_t width, size_t lines) {
+  char *d = static_cast<char *>(dst);
+  const char *s = static_cast<const char *>(src);
+  const size_t total = width * lines;
+  const unsigned hw = std::max(1u, std::thread::hardware_concurrency());
+  const size_t nt = std::min<size_t>({16, hw, std::max<size_t>(1, total >> 22)});  // >= 4 MiB per thread
+  auto part = [&](size_t i) {
+    if (dpitch == width && spitch == width) {
+      const size_t b0 = total * i / nt, b1 = total * (i + 1) / nt;
+      memcpy(d + b0, s + b0, b1 - b0);
+    } else {
+      for (size_t l = lines * i / nt, l1 = lines * (i + 1) / nt; l < l1; ++l)
+        memcpy(d + l * dpitch, s + l * spitch, width);
+    }
+  };
+  std::vector<std::thread> th;
+  for (size_t i = 1; i < nt; ++i) th.emplace_back(part, i);
+  part(0);
+  for (auto &t : th) t.join();
+}
+
+}  // namespace
+
+bool host_alloc_contains(const void *p, size_t bytes) { return in_host_alloc(p, bytes); }
+
+cudaError_t host_copy2d(uvatrmm_handle_t h, void *dst, size_t dpitch, const void *src, size_t spitch, size_t width,
+                        size_t height, cudaMemcpyKind kind) {
+  if (width == 0 || height == 0) return cudaSuccess;
+  const bool h2d = kind == cudaMemcpyHostToDevice;
+  const void *host = h2d ? src : dst;
+  const size_t hpitch = h2d ? spitch : dpitch;
+  const size_t extent = hpitch * (height - 1) + width;
+  const bool flat = dpitch == width && spitch == width;
+  // Direct DMA: operands in uvatrmm_host_alloc memory, small copies, or lines
+  // longer than a staging chunk.
+  if (in_host_alloc(host, extent) || width * height < ((size_t)1 << 20) || (!flat && width > h->hstage_bytes)) {
+    if (flat) return cudaMemcpyAsync(dst, src, width * height, kind, h->stream);
+    return cudaMemcpy2DAsync(dst, dpitch, src, spitch, width, height, kind, h->stream);
+  }
+  if (h->hstage_cap < h->hstage_bytes) {
+    release_host_staging(h);
+    size_t len = 0;
+    for (int b = 0; b < 2; ++b) {
+      if (map_region(h->hstage_bytes, &h->hstage[b], &len) != UVATRMM_OK) return cudaErrorMemoryAllocation;
+      cudaError_t e = cudaEventCreateWithFlags(&h->hstage_ev[b], cudaEventDisableTiming);
+      if (e != cudaSuccess) return e;
+    }
+    h->hstage_cap = h->hstage_bytes;
+  }
+  // A chunk is `lpc` lines (or, for a flat copy, `lpc` bytes of one line).
+  const size_t unit = flat ? 1 : width, count = flat ? width * height : height;
+  const size_t lpc = std::max<size_t>(1, h->hstage_bytes / unit);
+  const size_t nchunk = (count + lpc - 1) / lpc;
+  auto rows = [&](size_t k) { return std::min(lpc, count - k * lpc); };
+  cudaError_t e = cudaSuccess;
+  if (h2d) {
+    const char *s = static_cast<const char *>(src);
+    char *d = static_cast<char *>(dst);
+    for (size_t k = 0; k < nchunk && e == cudaSuccess; ++k) {
+      const int b = (int)(k & 1);
+      e = cudaEventSynchronize(h->hstage_ev[b]);  // the DMA that last read this buffer
+      if (e != cudaSuccess) break;
+      const size_t n = rows(k);
+      if (flat) {
+        par_copy(h->hstage[b], n, s + k * lpc, n, n, 1);
+        e = cudaMemcpyAsync(d + k * lpc, h->hstage[b], n, kind, h->stream);
+      } else {
+        par_copy(h->hstage[b], width, s + k * lpc * spitch, spitch, width, n);
+        e = cudaMemcpy2DAsync(d + k * lpc * dpitch, dpitch, h->hstage[b], width, width, n, kind, h->stream);
+      }
+      if (e == cudaSuccess) e = cudaEventRecord(h->hstage_ev[b], h->stream);
+    }
+    return e;
+  }
+  const char *s = static_cast<const char *>(src);
+  char *d = static_cast<char *>(dst);
+  auto issue = [&](size_t k) {
+    const int b = (int)(k & 1);
+    const size_t n = rows(k);
+    cudaError_t r = flat ? cudaMemcpyAsync(h->hstage[b], s + k * lpc, n, kind, h->stream)
+                         : cudaMemcpy2DAsync(h->hstage[b], width, s + k * lpc * spitch, spitch, width, n, kind,
+                                             h->stream);
+    return r == cudaSuccess ? cudaEventRecord(h->hstage_ev[b], h->stream) : r;
+  };
+  e = issue(0);
+  for (size_t k = 0; k < nchunk && e == cudaSuccess; ++k) {
+    if (k + 1 < nchunk) e = issue(k + 1);  // into the buffer unpacked at step k - 1
+    if (e == cudaSuccess) e = cudaEventSynchronize(h->hstage_ev[k & 1]);
+    if (e != cudaSuccess) break;
+    const size_t n = rows(k);
+    if (flat) par_copy(d + k * lpc, n, h->hstage[k & 1], n, n, 1);
+    else par_copy(d + k * lpc * dpitch, dpitch, h->hstage[k & 1], width, width, n);
+  }
+  return e;
+}
+
+void release_host_staging(uvatrmm_handle_t h) {
+  for (int b = 0; b < 2; ++b) {
+    if (h->hstage_ev[b]) {
+      cudaEventSynchronize(h->hstage_ev[b]);
+      cudaEventDestroy(h->hstage_ev[b]);
+      h->hstage_ev[b] = nullptr;
+    }
+    if (h->hstage[b]) {
+      uvatrmm_host_free(h->hstage[b]);
+      h->hstage[b] = nullptr;
+    }
+  }
+  h->hstage_cap = 0;
+}
+
+}  // namespace uvt
+
+using namespace uvt;
+
+extern "C" {
+
+UVATRMM_API int uvatrmm_host_alloc(size_t bytes, void **ptr) {
+  if (!ptr) return fail(UVATRMM_EINVAL, "ptr is NULL");
+  *ptr = nullptr;
+  size_t len = 0;
+  const int rc = map_region(bytes, ptr, &len);
+  return rc == UVATRMM_OK ? ok() : rc;
 }
 
 UVATRMM_API int uvatrmm_host_free(void *ptr) {

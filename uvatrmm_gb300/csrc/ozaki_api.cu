@@ -219,14 +219,14 @@ UVATRMM_API int uvatrmm_ozaki_dtrmm(uvatrmm_handle_t h, int layout, int side, in
   double *dA = static_cast<double *>(workspace(h, 0, (size_t)la * ka * 8));
   double *dB = static_cast<double *>(workspace(h, 2, (size_t)lb * t.n * 8));
   if (!dA || !dB) return uvatrmm_last_status();
-  cudaError_t e = cudaMemcpy2DAsync(dA, la * 8, A, lda * 8, ka * 8, ka, cudaMemcpyHostToDevice, h->stream);
-  if (e == cudaSuccess) e = cudaMemcpy2DAsync(dB, lb * 8, B, ldb * 8, t.m * 8, t.n, cudaMemcpyHostToDevice, h->stream);
+  cudaError_t e = host_copy2d(h, dA, la * 8, A, lda * 8, ka * 8, ka, cudaMemcpyHostToDevice);
+  if (e == cudaSuccess) e = host_copy2d(h, dB, lb * 8, B, ldb * 8, t.m * 8, t.n, cudaMemcpyHostToDevice);
   if (e != cudaSuccess) return cuda_fail(e, "host to device copy");
   int rc = ozaki_device(h, CblasColMajor, t.side, t.uplo, t.trans ? CblasTrans : CblasNoTrans,
                         t.unit ? CblasUnit : CblasNonUnit, t.m, t.n, t.alpha, dA, la, dB, lb, moduli, relerr_out,
                         bits_out);
   if (rc != UVATRMM_OK) return rc;
-  e = cudaMemcpy2DAsync(B, ldb * 8, dB, lb * 8, t.m * 8, t.n, cudaMemcpyDeviceToHost, h->stream);
+  e = host_copy2d(h, B, ldb * 8, dB, lb * 8, t.m * 8, t.n, cudaMemcpyDeviceToHost);
   if (e != cudaSuccess) return cuda_fail(e, "device to host copy");
   rc = collect_status(h);
   return rc == UVATRMM_OK ? ok() : rc;
