@@ -105,8 +105,13 @@ void par_copy(void *dst, size_t dpitch, const void *src, size_t spitch, size_t w
     }
   };
   std::vector<std::thread> th;
-  for (size_t i = 1; i < nt; ++i) th.emplace_back(part, i);
+  size_t started = 1;
+  try {
+    for (; started < nt; ++started) th.emplace_back(part, started);
+  } catch (...) {  // no thread available: the caller copies the remaining parts
+  }
   part(0);
+  for (size_t i = started; i < nt; ++i) part(i);
   for (auto &t : th) t.join();
 }
 
