@@ -168,6 +168,25 @@ __device__ __forceinline__ void tma_load_2d_mc(void *smem_dst, const CUtensorMap
       : "memory");
 }
 
+// ---------------------------------------------------------------- packed fp32 fold
+__device__ __forceinline__ uint64_t pack2(float f) {
+  uint64_t r;
+  asm("mov.b64 %0, {%1, %1};" : "=l"(r) : "f"(f));
+  return r;
+}
+// (a, b) := (a, b) - m * q with q = x * fl(1/m) rounded to an integer: the
+// fma with 1.5 * 2^23 rounds the exact product once (|x / m| < 2^22 for the
+// |x| < 2^24 held here) and x - q * m is exact; fl(1/m) is off by at most
+// 2^-24 relative, so |result| <= m/2 + 2.
+__device__ __forceinline__ void fold2(uint32_t &a, uint32_t &b, uint64_t inv2, uint64_t negm2) {
+  uint64_t x, q;
+  asm("mov.b64 %0, {%1, %2};" : "=l"(x) : "r"(a), "r"(b));
+  asm("fma.rn.f32x2 %0, %1, %2, %3;" : "=l"(q) : "l"(x), "l"(inv2), "l"(0x4B4000004B400000ull));
+  asm("sub.rn.f32x2 %0, %1, %2;" : "=l"(q) : "l"(q), "l"(0x4B4000004B400000ull));
+  asm("fma.rn.f32x2 %0, %1, %2, %3;" : "=l"(x) : "l"(q), "l"(negm2), "l"(x));
+  asm("mov.b64 {%0, %1}, %2;" : "=r"(a), "=r"(b) : "l"(x));
+}
+
 // ---------------------------------------------------------------- tcgen05 wrappers
 __device__ __forceinline__ uint64_t sw128_desc(uint32_t saddr) {
   uint64_t d = (uint64_t)((saddr & 0x3FFFFu) >> 4);
@@ -377,6 +396,7 @@ __global__ void __cluster_dims__(PAIR, 1, 1) __launch_bounds__(NUM_THREADS, 1)
       const int nslab = T.ks1 - T.ks0;
       const int nchunk = (nslab + CHUNK_SLABS - 1) / CHUNK_SLABS;
       const float m = p.mod_f[T.l], inv = p.inv_f[T.l], cu = p.u_f[P.nmod][T.l];
+      const uint64_t inv2 = pack2(inv), negm2 = pack2(-m);
       // This thread's row of the tile's residue output (column stride Mp).
       uint16_t *out = P.res + (int64_t)T.l * P.plane + ((int64_t)T.tp * PAIR + rank) * BM + row;
       uint32_t *r1 = r1s + row;  // this row's words of r1s, stride BM (each thread touches only its own)
@@ -391,17 +411,15 @@ __global__ void __cluster_dims__(PAIR, 1, 1) __launch_bounds__(NUM_THREADS, 1)
         tc_fence_after();
         const uint32_t tb = lane_base + b * (uint32_t)BN;
         if (c + 2 < nchunk) {
-          // Fold: acc := acc - m * rint(acc / m), exact in fp32.
+          // Fold: acc := acc - m * q, q = x / m rounded to nearest, exact in
+          // fp32, two values per packed instruction.
 #pragma unroll 1
           for (int cb = cb0; cb < cb0 + CB_PER_WARP; ++cb) {
             uint32_t v[32];
             tmem_ld32(tb + (uint32_t)(cb * 32), v);
             tmem_wait_ld();
 #pragma unroll
-            for (int e = 0; e < 32; ++e) {
-              const float x = __uint_as_float(v[e]);
-              v[e] = __float_as_uint(fmaf(-rintf(x * inv), m, x));
-            }
+            for (int e = 0; e < 32; e += 2) fold2(v[e], v[e + 1], inv2, negm2);
             tmem_st32(tb + (uint32_t)(cb * 32), v);
           }
           tmem_wait_st();
