@@ -270,14 +270,14 @@ __device__ __forceinline__ double times_pow2(double d, int k) {
 }
 
 // One element from its residues (16-bit field `f` of the pairs rw[l]) -> C value (alpha applied).
-template <int L>
-__device__ __forceinline__ double crt_element(const CrtConst &cc, const uint2 (&rw)[kMaxModuli], int f, int er,
+template <int L, int NM>
+__device__ __forceinline__ double crt_element(const CrtConst &cc, const uint2 (&rw)[NM], int f, int er,
                                               int ec, double alpha, bool unit_alpha) {
   uint64_t acc[L];
 #pragma unroll
   for (int k = 0; k < L; ++k) acc[k] = 0;
 #pragma unroll
-  for (int l = 0; l < kMaxModuli; ++l) {
+  for (int l = 0; l < NM; ++l) {
     if (l < cc.n) {
       const uint32_t y = ((f < 2 ? rw[l].x : rw[l].y) >> (16 * (f & 1))) & 0xFFFFu;
 #pragma unroll
@@ -363,7 +363,9 @@ __device__ __forceinline__ double crt_element(const CrtConst &cc, const uint2 (&
 // thread takes four consecutive rows (one 8-byte load per residue plane).
 constexpr int kCrtRows = 4;
 
-template <int L>
+// NM >= n bounds the unrolled modulus loops (the CRT set's size rounded up to
+// a multiple of 4 for single calls, kMaxModuli for grouped ones).
+template <int L, int NM>
 __device__ __forceinline__ void reassemble_body(const CrtConst &cc, const uint16_t *res, int64_t Mp, int64_t plane,
                                                 int64_t M, int64_t N, const int *e_row, const int *e_col,
                                                 double alpha, double *C, int64_t ldc, int64_t bx, int64_t j0,
@@ -375,10 +377,10 @@ __device__ __forceinline__ void reassemble_body(const CrtConst &cc, const uint16
   const int er[kCrtRows] = {er4.x, er4.y, er4.z, er4.w};
   for (int64_t j = j0; j < N; j += jstep) {
     const int ec = e_col[j];
-    uint2 rw[kMaxModuli];
+    uint2 rw[NM];
     const uint16_t *rp = res + j * Mp + i0;
 #pragma unroll
-    for (int l = 0; l < kMaxModuli; ++l)
+    for (int l = 0; l < NM; ++l)
       rw[l] = l < cc.n ? *reinterpret_cast<const uint2 *>(rp + l * plane) : make_uint2(0u, 0u);
     // One row at a time: interleaving the four rows' limb sums doubles the
     // registers and halves the resident blocks.
@@ -388,18 +390,18 @@ __device__ __forceinline__ void reassemble_body(const CrtConst &cc, const uint16
       const int erq = q == 0 ? er[0] : q == 1 ? er[1] : q == 2 ? er[2] : er[3];
       double v;
       if (erq == kExpNone || ec == kExpNone) v = alpha * 0.0;
-      else v = crt_element<L>(cc, rw, q, erq, ec, alpha, unit_alpha);
+      else v = crt_element<L, NM>(cc, rw, q, erq, ec, alpha, unit_alpha);
       C[i0 + q + j * ldc] = v;
     }
   }
 }
 
-template <int L>
+template <int L, int NM>
 __global__ void __launch_bounds__(256) reassemble_kernel(const __grid_constant__ CrtConst cc, const uint16_t *res,
                                                          int64_t Mp, int64_t plane, int64_t M, int64_t N,
                                                          const int *e_row, const int *e_col, double alpha,
                                                          double *C, int64_t ldc) {
-  reassemble_body<L>(cc, res, Mp, plane, M, N, e_row, e_col, alpha, C, ldc, blockIdx.x, blockIdx.y, gridDim.y);
+  reassemble_body<L, NM>(cc, res, Mp, plane, M, N, e_row, e_col, alpha, C, ldc, blockIdx.x, blockIdx.y, gridDim.y);
 }
 
 // ---------------------------------------------------------------- grouped (wave) kernels
@@ -466,8 +468,8 @@ __global__ void __launch_bounds__(256) reassemble_wave_kernel(const CrtJob *jobs
   switch (cc.limbs) {
 #define UVT_CRT_CASE(L)                                                                                           \
   case L:                                                                                                         \
-    reassemble_body<L>(cc, J.res, J.Mp, J.plane, J.M, J.N, J.e_row, J.e_col, J.alpha, J.C, J.ldc, lb % J.gx,      \
-                       lb / J.gx, J.N);                                                                           \
+    reassemble_body<L, kMaxModuli>(cc, J.res, J.Mp, J.plane, J.M, J.N, J.e_row, J.e_col, J.alpha, J.C, J.ldc, \
+                                   lb % J.gx, lb / J.gx, J.N);                                                   \
     break;
     UVT_CRT_CASE(2) UVT_CRT_CASE(3) UVT_CRT_CASE(4) UVT_CRT_CASE(5) UVT_CRT_CASE(6)
 #undef UVT_CRT_CASE
@@ -669,13 +671,15 @@ int oz_reassemble(const OzPlan &plan, const uint16_t *res, const int *e_row, con
   const CrtConst cc = make_crt(plan);
   if (plan.M <= 0 || plan.N <= 0) return UVATRMM_OK;
   dim3 grid((unsigned)((plan.M + 256 * kCrtRows - 1) / (256 * kCrtRows)), (unsigned)std::min<int64_t>(plan.N, 65535));
-  switch (cc.limbs) {
-#define UVT_CRT_LAUNCH(L)                                                                                         \
-  case L:                                                                                                         \
-    reassemble_kernel<L><<<grid, 256, 0, st>>>(cc, res, plan.Mp, plan.Mp * plan.Np, plan.M, plan.N, e_row, e_col, \
-                                               alpha, C, ldc);                                                    \
+  const int nm = (cc.n + 3) / 4 * 4;
+  switch (nm * 8 + cc.limbs) {
+#define UVT_CRT_LAUNCH(NM, L)                                                                                     \
+  case NM * 8 + L:                                                                                                \
+    reassemble_kernel<L, NM><<<grid, 256, 0, st>>>(cc, res, plan.Mp, plan.Mp * plan.Np, plan.M, plan.N, e_row,    \
+                                                   e_col, alpha, C, ldc);                                         \
     break;
-    UVT_CRT_LAUNCH(2) UVT_CRT_LAUNCH(3) UVT_CRT_LAUNCH(4) UVT_CRT_LAUNCH(5) UVT_CRT_LAUNCH(6)
+    UVT_CRT_LAUNCH(4, 2) UVT_CRT_LAUNCH(8, 2) UVT_CRT_LAUNCH(8, 3) UVT_CRT_LAUNCH(12, 3) UVT_CRT_LAUNCH(12, 4)
+    UVT_CRT_LAUNCH(16, 4) UVT_CRT_LAUNCH(16, 5) UVT_CRT_LAUNCH(20, 5) UVT_CRT_LAUNCH(20, 6)
 #undef UVT_CRT_LAUNCH
     default: return UVATRMM_EINVAL;
   }
