@@ -18,9 +18,14 @@ needed between steps.  TFLOP/s counts m^2*n flops.
             + add per row block, UVaTRMM/src/mm_triangular.c:319-403) restated in
             oracle/ over OpenBLAS, one rank's column slice of the P=4 balanced
             run, all host cores
+After the headline the line carries single-GPU sections (Ozaki precision
+sweep, the plain-path variants with their checks, GEMM / stage / layout
+rows, grouped batch, serving sweep) and ends with a compact `summary`
+(checks, Ozaki, serving).
 --impl reference: the same CPU implementation timed per step on that sample.
-N>1 (torchrun): independent replicas, one per GPU (the reference's column
-split makes replicas the natural scaling; there is no data exchange).
+N>1 (torchrun): independent replicas of the headline TRMM, one per GPU (the
+reference's column split makes replicas the natural scaling; there is no
+data exchange); the single-GPU sections are skipped and the line says so.
 """
 from __future__ import annotations
 
@@ -42,6 +47,49 @@ FP64_FLOP_PER_CLK_SM = 4.0
 # DRAM bytes per flop of the FP64 kernel measured by ncu at m = n = 4096
 # (1.2965e9 B over 4096^3 flops); B panels are re-read per row tile.
 TRAFFIC_BYTES_PER_FLOP = 1.2965e9 / 4096.0 ** 3
+TRAFFIC_SOURCE = "ncu dram bytes per launch at m=n=4096, scaled by flops to this size"
+
+
+def headline_config(m, n, ws):
+    """The headline workload; both arms report this same config."""
+    return {"workload": f"plain FP64 TRMM m=n={m}, side=L uplo=L trans=N diag=N alpha=1, "
+                        "A and B uniform[-1,1) seed 1", "m": m, "n": n,
+            "l2": "inputs larger than L2 (no flush needed)", "parallelism": f"replicas{ws}"}
+
+
+def _sig(x, d=3):
+    return None if x is None else float(f"{x:.{d}g}")
+
+
+def summary(out):
+    """Compact end of the JSON line: the checks, the Ozaki figures and the serving result."""
+    s = {}
+    chk = {"headline_rel_err": _sig(out.get("check", {}).get("sampled_rel_fro_err_vs_openblas"))}
+    var = out.get("variants")
+    if var:
+        cases = {f'{c["uplo"]} {c["schedule/shape"]}': _sig(c.get("rel_err")) for c in var["cases"]}
+        for k in ("dmma_engine", "skinny", "large"):
+            if k in var:
+                cases[k] = _sig(var[k].get("rel_err"))
+        chk["variants_rel_err"] = cases
+    chk["tol_8_k_eps"] = _sig(out.get("check", {}).get("tol"))
+    s["check"] = chk
+    oz = out.get("ozaki")
+    if oz:
+        s["ozaki"] = {"tflops": oz["value"], "x_plain": oz["speedup_vs_plain_fp64"], "moduli": oz["moduli"],
+                      "bits": oz["bits"], "rel_err_dd": _sig(oz["rel_fro_err_vs_dd_oracle"]),
+                      "lib_rel_err_host_fp64": _sig(oz.get("library_relerr_vs_host_fp64")),
+                      "gemm_tflops": oz["roofline"]["achieved"], "gemm_frac": oz["roofline"]["frac"],
+                      "sm_mhz": oz["clocks"].get("sm_mhz"), "reasons": oz["clocks"].get("reasons"),
+                      "int8_sweep": [[e.get("int8_slices"), e["moduli"], e["bits"], _sig(e["rel_fro_err_vs_dd_oracle"])]
+                                     for e in oz["slice_sweep"]]}
+    sv = out.get("serving")
+    if sv:
+        s["serving"] = {"max_steady_rate": sv["max_steady_rate_req_per_s"], "alone_p99_ms": sv["alone_p99_ms"],
+                        "rate_p50_p99_p99h1_p99h2_tflops": [
+                            [r["rate_req_per_s"], _sig(r["p50_ms"]), _sig(r["p99_ms"]), _sig(r["p99_first_half_ms"]),
+                             _sig(r["p99_second_half_ms"]), r["sustained_tflops"]] for r in sv["rates"]]}
+    return s
 
 
 def dist_env():
@@ -185,9 +233,6 @@ def run_gpu(args, ws, rank, local):
     for _ in range(args.warmup):
         step()
     h.sync()
-    # FP64 peak probes run hot, right after the warm-up steps.
-    peak_dfma = h.probe_fp64_peak(u.ENGINE_DFMA)
-    peak_dmma = h.probe_fp64_peak(u.ENGINE_DMMA)
     if ws > 1:
         torch.distributed.barrier()
     torch.cuda.synchronize(dev)
@@ -273,10 +318,8 @@ def run_gpu(args, ws, rank, local):
         "metric": METRIC, "value": round(value, 4), "unit": "TFLOP/s", "n_gpus": ws, "steps": args.steps,
         "warmup": args.warmup, "ms_per_step": round(total_ms / args.steps, 3), "higher_is_better": True,
         "scaling": "weak", "vs_baseline": None, "dtype": "f64", "data": "synthetic (seeded uniform[-1,1), seed 1)",
-        "config": {"workload": f"plain FP64 TRMM m=n={m}, side=L uplo=L trans=N diag=N alpha=1, "
-                               "dynamic schedule, trapezoid tiles", "m": m, "n": n,
-                   "engine": "DFMA", "l2": "inputs larger than L2 (no flush needed)",
-                   "parallelism": f"replicas{ws}"},
+        "config": headline_config(m, n, ws),
+        "kernel": {"engine": "DFMA", "schedule": "dynamic", "shape": "trapezoid"},
         "e2e": {"value": round(e2e_value, 4), "unit": "TFLOP/s", "h2d_bytes_per_step": 8 * (m * m + m * n),
                 "d2h_bytes_per_step": 8 * m * n, "api": "uvatrmm_dtrmm_async on two handles (host operands from uvatrmm_host_alloc, B "
                        "double-buffered), every step copying A and B in and B out",
@@ -288,22 +331,37 @@ def run_gpu(args, ws, rank, local):
                      "traffic": TRAFFIC_BYTES_PER_FLOP * flops if m == n else None,
                      "peak_source": f"FP64 issue limit {FP64_FLOP_PER_CLK_SM} flop/clk/SM x {n_sms} SMs x "
                                     f"{sm_mhz:.0f} MHz (sampled); MEASURED_PEAKS.json has no FP64 figure; "
-                                    f"in-run probe kernels: DFMA {peak_dfma:.3f}, DMMA {peak_dmma:.3f} TFLOP/s; "
                                     f"nominal GB300 FP64 {NOMINAL_FP64_TFLOPS}",
                      "frac_of_nominal": round(achieved / NOMINAL_FP64_TFLOPS, 4),
-                     "traffic_source": "dram bytes per launch scaled by flops from the m=4096 ncu capture "
-                                       "(profiles/trmm_fp64_dfma_m16384.md)"},
+                     "traffic_source": TRAFFIC_SOURCE},
         "gpu_launches": args.steps,
         "clocks": clocks,
-        "check": {"sampled_rel_fro_err_vs_openblas": relerr},
+        "check": {"sampled_rel_fro_err_vs_openblas": relerr, "tol": 8 * m * 2.0 ** -52},
     }
     del hA, hBs, hB0
+    out.update(run_sections(args, ws, rank, h, dev, stream, achieved, peak))
+    return out
+
+
+SINGLE_GPU_SECTIONS = ("ozaki", "variants", "next_rows", "batch", "serving")
+
+
+def run_sections(args, ws, rank, h, dev, stream, plain_tflops, fp64_peak):
+    """The sections after the headline.  They are single-GPU measurements:
+    under torchrun (ws > 1) every rank runs the headline replica only and the
+    line records which sections were skipped."""
+    import uvatrmm_gb300 as u
+    out = {}
+    if ws > 1:
+        out["sections_skipped"] = {"sections": list(SINGLE_GPU_SECTIONS),
+                                   "why": "single-GPU sections; at N > 1 each rank runs the plain FP64 replica only"}
+        return out
     if not args.no_ozaki:
-        out["ozaki"] = run_ozaki(args, h, dev, stream, rank, achieved)
+        out["ozaki"] = run_ozaki(args, h, dev, stream, rank, plain_tflops)
     if args.variants:
-        out["variants"] = run_variants(args, h, dev, stream, peak)
+        out["variants"] = run_variants(args, h, dev, stream, fp64_peak)
     if args.next_n > 0:
-        out["next_rows"] = run_next_rows(args, h, dev, stream, peak)
+        out["next_rows"] = run_next_rows(args, h, dev, stream, fp64_peak)
     if args.batch > 0:
         hb = u.Handle(stream=stream)  # its own workspace for the one-call-per-problem comparison
         out["batch"] = run_batch(args, hb, dev, stream)
@@ -343,10 +401,20 @@ def serve_requests(count, seed, dev, h):
     return reqs, rng
 
 
+def _pct(v, q):
+    import numpy as np
+    return round(float(np.percentile(v, q)), 3) if len(v) else None
+
+
 def run_serving(args, h, dev, stream):
     """Poisson arrivals into the server (device-resident operands, 120 GB
-    budget) at each rate; p50/p99 latency and sustained TFLOP/s, beside the
-    same requests run one at a time through the direct entry points."""
+    budget) at rates up to about the device's capacity, each for
+    `serve_seconds` of arrivals; requests cycle through a pool of distinct
+    operand sets (a set is reused once its previous request is done).
+    Per-request latencies give p50 / p99 over the stream and p99 over each
+    half of it: a queue that grows shows as a second half slower than the
+    first.  Beside them, the same requests one at a time through the direct
+    entry points."""
     import numpy as np
     import torch
 
@@ -362,37 +430,57 @@ def run_serving(args, h, dev, stream):
         (h.ozaki_device if p["tier"] == u.TIER_OZAKI else h.dtrmm_device)(*a)
         h.sync()
         alone_ms.append((time.perf_counter() - t0) * 1e3)
+    alone_p99 = _pct(alone_ms, 99)
     rates = []
     for rate in args.serve_rates:
+        count = max(1, int(round(rate * args.serve_seconds)))
         srv = u.Server(h, hbm_budget_bytes=int(120e9))
-        gaps = rng.exponential(1.0 / rate, size=len(reqs))
-        ids = []
+        gaps = rng.exponential(1.0 / rate, size=count)
+        ids, last = [], {}
         t_next = time.perf_counter()
-        for p, gap in zip(reqs, gaps):
-            t_next += gap
+        for i in range(count):
+            k = i % len(reqs)
+            if k in last:
+                srv.wait(last[k])
+            t_next += gaps[i]
             while True:
                 d = t_next - time.perf_counter()
                 if d <= 0:
                     break
                 time.sleep(min(d, 0.001) if d > 0.0002 else 0)
-            ids.append(srv.submit(p))
+            last[k] = srv.submit(reqs[k])
+            ids.append(last[k])
         bad = sum(srv.wait(r) != 0 for r in ids)
+        lat = [x for x in (srv.latency_ms(r) for r in ids) if x is not None]
         st = srv.stats()
         srv.close()
         span = st["last_done_s"] - st["first_submit_s"]
-        rates.append({"rate_req_per_s": rate, "requests": len(ids), "failed": bad,
-                      "p50_ms": round(st["p50_ms"], 3), "p99_ms": round(st["p99_ms"], 3),
-                      "mean_ms": round(st["mean_ms"], 3), "max_ms": round(st["max_ms"], 3),
+        half = len(lat) // 2
+        served = sum(flops[i % len(reqs)] for i in range(count))
+        rates.append({"rate_req_per_s": rate, "requests": count, "failed": bad,
+                      "p50_ms": _pct(lat, 50), "p99_ms": _pct(lat, 99),
+                      "p99_first_half_ms": _pct(lat[:half], 99), "p99_second_half_ms": _pct(lat[half:], 99),
+                      "mean_ms": round(float(np.mean(lat)), 3) if lat else None, "max_ms": round(max(lat), 3),
+                      "offered_tflops": round(served / (count / rate) / 1e12, 4),
                       "sustained_tflops": round(st["served_flops"] / span / 1e12, 4), "ticks": st["ticks"],
                       "peak_pool_gib": round(st["peak_bytes"] / 2 ** 30, 2)})
+    # Highest rate served in steady state: no failures, p99 within 2x the
+    # one-at-a-time p99, and the second half's p99 within 1.5x the first's.
+    ok = [r["rate_req_per_s"] for r in rates
+          if r["failed"] == 0 and r["p99_ms"] <= 2.0 * alone_p99
+          and r["p99_second_half_ms"] <= 1.5 * r["p99_first_half_ms"]]
     del reqs
     torch.cuda.empty_cache()
-    return {"workload": f"{args.serve} requests per rate, m logU[128,8192], n logU[32,8192], 50% FP64 / 50% "
-                        "Ozaki (<=1e-14), Poisson arrivals, 120 GB budget, device-resident operands, seed 4",
-            "alone_p50_ms": round(float(np.percentile(alone_ms, 50)), 3),
-            "alone_p99_ms": round(float(np.percentile(alone_ms, 99)), 3),
+    return {"workload": f"Poisson arrivals for {args.serve_seconds:g} s per rate over a pool of {args.serve} "
+                        "request operand sets, m logU[128,8192], n logU[32,8192], 50% FP64 / 50% Ozaki (<=1e-14), "
+                        "side/uplo/trans uniform, 120 GB budget, device-resident operands, seed 4",
+            "alone_p50_ms": _pct(alone_ms, 50), "alone_p99_ms": alone_p99,
             "alone_requests": len(alone_ms),
-            "total_gflop_per_pass": round(sum(flops) / 1e9, 1), "rates": rates}
+            "alone_capacity_req_per_s": round(1e3 / float(np.mean(alone_ms)), 1),
+            "mean_gflop_per_request": round(sum(flops) / len(flops) / 1e9, 2),
+            "max_steady_rate_req_per_s": max(ok) if ok else None,
+            "steady_rule": "no failures, p99 <= 2x alone p99, second-half p99 <= 1.5x first-half p99",
+            "rates": rates}
 
 
 def batch_problems(count, seed, dev, h):
@@ -488,33 +576,68 @@ def _timed(stream, fn, steps, warm=True):
     return statistics.mean(times)
 
 
+def _sample_cols(d, rows, ld, cols):
+    """Columns `cols` of a column-major device matrix as a host (rows x len(cols)) array."""
+    import numpy as np
+    return np.stack([d[j * ld:j * ld + rows].cpu().numpy() for j in cols], axis=1)
+
+
+def _openblas_cols(A, m, uplo, Bcols):
+    """OpenBLAS cblas_dtrmm (left, no-trans, non-unit, alpha 1) of sampled B
+    columns (an m x k host array); A is the flat column-major m x m operand."""
+    import numpy as np
+
+    import uvatrmm_gb300 as u
+    from oracle import oracle as orc
+    k = Bcols.shape[1]
+    flat = np.ascontiguousarray(Bcols.T).ravel()  # column-major m x k, ld m
+    orc.blas_dtrmm(u.COL, u.LEFT, uplo, u.NOTRANS, u.NONUNIT, m, k, 1.0, A, m, flat, m)
+    return flat.reshape(k, m).T
+
+
+def _rel(got, ref):
+    import numpy as np
+    return float(np.linalg.norm(got - ref) / np.linalg.norm(ref))
+
+
 def run_variants(args, h, dev, stream, fp64_peak):
     """The plain FP64 configuration's other cases: both uplo under every schedule and
-    message shape at m = n = 16384, the skinny m = 16384, n = 256 case, and m = n = 32768."""
+    message shape at m = n = 16384, the skinny m = 16384, n = 256 case, and m = n = 32768.
+    Every case's output is checked on four sampled columns against OpenBLAS
+    cblas_dtrmm (tolerance 8 k eps relative Frobenius)."""
     import torch
 
     import uvatrmm_gb300 as u
     hbm, _ = hbm_peak()
-    out = {"cases": []}
+    out = {"cases": [], "tol": 8 * args.n * 2.0 ** -52}
     m = args.n
+    sel = [0, m // 3, m // 2, m - 1]
     dA = torch.empty(m * m, dtype=torch.float64, device=dev)
     dB = torch.empty(m * m, dtype=torch.float64, device=dev)
     dC = torch.empty_like(dB)
     h.gen_uniform(1, 1, m, m, dB, 1, m)
+    h.sync()
+    Bs = _sample_cols(dB, m, m, sel)
     combos = [(u.SCHED_DYNAMIC, u.SHAPE_TRAPEZOID, "dynamic/trapezoid"), (u.SCHED_REG, u.SHAPE_BOXES, "reg/boxes"),
               (u.SCHED_REG, u.SHAPE_TRAPEZOID, "reg/trapezoid"), (u.SCHED_BALANCED, u.SHAPE_BOXES, "balanced/boxes"),
               (u.SCHED_BALANCED, u.SHAPE_TRAPEZOID, "balanced/trapezoid")]
+    ref = None
     for uplo, uname in ((u.LOWER, "L"), (u.UPPER, "U")):
         h.gen_uniform(1, 0, m, m, dA, 1, m, tri=uname)
         h.sync()
+        if args.check:
+            ref = _openblas_cols(dA.cpu().numpy(), m, uplo, Bs)
         for sched, shape, name in combos:
             h.set_option("schedule", sched)
             h.set_option("shape", shape)
             ms = _timed(stream, lambda: h.dtrmm_device_oop(u.COL, u.LEFT, uplo, u.NOTRANS, u.NONUNIT, m, m, 1.0,
                                                            dA, m, dB, m, dC, m), 1, warm=False)
             tf = float(m) ** 3 / (ms * 1e-3) / 1e12
-            out["cases"].append({"m": m, "n": m, "uplo": uname, "schedule/shape": name, "tflops": round(tf, 4),
-                                 "frac_of_fp64_issue_limit": round(tf / fp64_peak, 4), "ms": round(ms, 2)})
+            case = {"m": m, "n": m, "uplo": uname, "schedule/shape": name, "tflops": round(tf, 4),
+                    "frac_of_fp64_issue_limit": round(tf / fp64_peak, 4), "ms": round(ms, 2)}
+            if ref is not None:
+                case["rel_err"] = _rel(_sample_cols(dC, m, m, sel), ref)
+            out["cases"].append(case)
     h.set_option("schedule", u.SCHED_DYNAMIC)
     h.set_option("shape", u.SHAPE_TRAPEZOID)
     # the FP64 tensor-core engine (DMMA, mma.sync m8n8k4) on the last uplo's operands
@@ -526,6 +649,8 @@ def run_variants(args, h, dev, stream, fp64_peak):
     out["dmma_engine"] = {"m": m, "n": m, "uplo": "U", "schedule/shape": "dynamic/trapezoid",
                           "tflops": round(tf, 4), "frac_of_fp64_issue_limit": round(tf / fp64_peak, 4),
                           "ms": round(ms, 2)}
+    if ref is not None:
+        out["dmma_engine"]["rel_err"] = _rel(_sample_cols(dC, m, m, sel), ref)
     # skinny: B is m x 256; bytes = A triangle + B read + C written
     ns = 256
     h.gen_uniform(1, 0, m, m, dA, 1, m, tri="L")
@@ -539,6 +664,10 @@ def run_variants(args, h, dev, stream, fp64_peak):
                      "ms": round(ms, 3),
                      "note": "arithmetic intensity n/4 = 64 flop/B, far above the FP64 ridge (~0.19 flop/B): "
                              "still bound by the FP64 pipe"}
+    if args.check:
+        ssel = [0, ns // 3, ns // 2, ns - 1]
+        out["skinny"]["rel_err"] = _rel(_sample_cols(dC, m, m, ssel),
+                                        _openblas_cols(dA.cpu().numpy(), m, u.LOWER, _sample_cols(dB, m, m, ssel)))
     del dA, dB, dC
     torch.cuda.empty_cache()
     if args.big_n > 0:
@@ -558,6 +687,11 @@ def run_variants(args, h, dev, stream, fp64_peak):
         tf = float(M) ** 3 / (ms * 1e-3) / 1e12
         out["large"] = {"m": M, "n": M, "tflops": round(tf, 4), "frac_of_fp64_issue_limit": round(tf / fp64_peak, 4),
                         "ms": round(ms, 1), "runs": 1, "note": "one timed call after the 16384 runs (warm kernel)"}
+        if args.check:
+            bsel = [0, M // 3, M // 2, M - 1]
+            out["large"]["rel_err"] = _rel(_sample_cols(dC, M, M, bsel),
+                                           _openblas_cols(dA.cpu().numpy(), M, u.LOWER, _sample_cols(dB, M, M, bsel)))
+            out["large"]["tol"] = 8 * M * 2.0 ** -52
         del dA, dB, dC
         torch.cuda.empty_cache()
     return out
@@ -669,6 +803,22 @@ def ozaki_mma_flops(m, n, moduli, side_left=True, lower=True):
     return 2.0 * BM * BN * total * moduli
 
 
+def int8_slice_map(k):
+    """INT8 digit-slice counts 5-9 (7 bits per signed 8-bit slice) mapped to the
+    fewest CRT moduli whose bits per scaled entry reach the same budget at
+    inner dimension k."""
+    import uvatrmm_gb300 as u
+    out = []
+    for sl in range(5, 10):
+        for mo in range(2, 21):
+            _, b = u.ozaki_plan(k, mo)
+            if b >= 7 * sl:
+                out.append({"int8_slices": sl, "int8_bits": 7 * sl, "int8_products": sl * (sl + 1) // 2,
+                            "moduli": mo})
+                break
+    return out
+
+
 def run_ozaki(args, h, dev, stream, rank, plain_tflops):
     """Ozaki emulated FP64 TRMM at the precision configuration: m = n = 32768,
     side=L, uplo=U, trans=T, entries uniform[-1,1) * 2^k, k uniform in
@@ -714,7 +864,15 @@ def run_ozaki(args, h, dev, stream, rank, plain_tflops):
     peak, peak_src = bf16_peak()
     gemm_tflops = gemm_flops / (st[2] * 1e-3) / 1e12
 
+    # The precision configuration sweeps INT8 digit-slice counts 5-9.  Signed
+    # 8-bit slices hold 7 bits each, so s slices keep 7s bits of a scaled
+    # entry (and need s(s+1)/2 INT8 products); the CRT form keeps t bits with
+    # N residue products.  Each s maps to the fewest moduli N with t >= 7s at
+    # this K; the automatic count and the widest set (20) are timed too.
+    slice_map = int8_slice_map(m)
+    settings = sorted({e["moduli"] for e in slice_map} | {moduli, 20})
     sweep = []
+    lib_err = None
     if rank == 0 and args.check:
         from oracle import oracle as orc
         sel = [1, n // 3, (2 * n) // 3, n - 2]
@@ -724,11 +882,18 @@ def run_ozaki(args, h, dev, stream, rank, plain_tflops):
         orc.lib()
         ref = orc.dtrmm_dd(C_, Le, Up, Tr, NU, m, len(sel), 1.0, A, m, Bs, m)
         del A
-        for mo in sorted({14, 15, 16, 17, 18, 19, 20, moduli}):
-            _, est, b = step(mo, want_err=True)
+        for mo in settings:
+            ms, _, b = step(mo)
             got = np.stack([dB[j * m:(j + 1) * m].cpu().numpy() for j in sel], axis=1)
-            sweep.append({"moduli": mo, "bits": b, "rel_fro_err_vs_dd_oracle": float(
-                np.linalg.norm(got - ref) / np.linalg.norm(ref)), "rel_fro_err_vs_plain_fp64_gpu": est})
+            e = {"moduli": mo, "bits": b, "ms": round(ms, 2),
+                 "rel_fro_err_vs_dd_oracle": float(np.linalg.norm(got - ref) / np.linalg.norm(ref))}
+            e.update({k: v for x in slice_map if x["moduli"] == mo for k, v in x.items() if k != "moduli"})
+            sweep.append(e)
+        # The library's own error report against its host FP64 reference (Dot2
+        # over 8 sampled columns), at the automatic count.
+        h.set_option("ozaki_err_host", 1)
+        _, lib_err, _ = step(0, want_err=True)
+        h.set_option("ozaki_err_host", 0)
     h.set_option("stage_timing", 0)
     h.set_option("ozaki_raster", 0)
     del dA, dB0, dB
@@ -740,6 +905,7 @@ def run_ozaki(args, h, dev, stream, rank, plain_tflops):
         "value": round(tflops, 3), "unit": "TFLOP/s (m^2 n FP64-equivalent flops)", "steps": len(times),
         "ms_per_step": round(t_ms, 3), "moduli": moduli, "bits": bits,
         "rel_fro_err_vs_dd_oracle": auto["rel_fro_err_vs_dd_oracle"] if auto else None,
+        "library_relerr_vs_host_fp64": lib_err,
         "speedup_vs_plain_fp64": round(tflops / plain_tflops, 2),
         "stage_ms": {"scaling": round(st[0], 3), "slicing": round(st[1], 3), "residue_gemm": round(st[2], 3),
                      "reassembly": round(st[3], 3)},
@@ -774,8 +940,9 @@ def main():
     ap.add_argument("--next-steps", type=int, default=3)
     ap.add_argument("--batch", type=int, default=2000)
     ap.add_argument("--batch-steps", type=int, default=2)
-    ap.add_argument("--serve", type=int, default=300)
-    ap.add_argument("--serve-rates", type=float, nargs="*", default=[100.0, 1000.0, 5000.0])
+    ap.add_argument("--serve", type=int, default=300, help="distinct request operand sets (0: no serving run)")
+    ap.add_argument("--serve-seconds", type=float, default=20.0, help="seconds of arrivals per rate")
+    ap.add_argument("--serve-rates", type=float, nargs="*", default=[50.0, 100.0, 150.0, 200.0])
     args = ap.parse_args()
     ws, rank, local = dist_env()
     threads = os.cpu_count() or 1
@@ -787,8 +954,7 @@ def main():
         line = {"impl": "reference", "metric": METRIC, "value": round(cb["value"], 5), "unit": "TFLOP/s",
                 "n_gpus": ws, "steps": args.steps, "warmup": args.warmup, "higher_is_better": True,
                 "scaling": "weak", "vs_baseline": None, "dtype": "f64", "data": "synthetic (seeded uniform[-1,1))",
-                "config": {"workload": f"plain FP64 TRMM m=n={args.n}, side=L uplo=L trans=N diag=N alpha=1",
-                           "m": args.n, "n": args.n},
+                "config": headline_config(args.n, args.n, ws),
                 "cpu_baseline": cb,
                 "e2e": {"value": round(cb["value"], 5), "unit": "TFLOP/s", "h2d_bytes_per_step": 0,
                         "d2h_bytes_per_step": 0}}
@@ -801,6 +967,8 @@ def main():
     out = run_gpu(args, ws, rank, local)
     if rank == 0 and not args.no_cpu_baseline:
         out["cpu_baseline"] = cpu_reference_sample(args.cpu_n, 1, 1, threads)
+    if rank == 0:
+        out["summary"] = summary(out)
     if ws > 1:
         import torch
         torch.distributed.barrier()

@@ -94,8 +94,16 @@ typedef enum {
   UVATRMM_OPT_AUTOTUNE = 7,         /* 1 (default): measure untuned shape buckets; 0: defaults only */
   UVATRMM_OPT_OZAKI_RASTER = 8,     /* Ozaki residue GEMM of single calls: major tiles per raster
                                        group (0 = default: 4 when m, n >= 16384, else 2; or 1..64) */
-  UVATRMM_OPT_HOST_STAGE_KB = 9     /* chunk of the host staging used for host operands outside
+  UVATRMM_OPT_HOST_STAGE_KB = 9,    /* chunk of the host staging used for host operands outside
                                        uvatrmm_host_alloc memory, KiB (0 = default 262144; >= 64) */
+  UVATRMM_OPT_WAIT_EXPIRY_TEST = 10,/* tests of the failure path only: 0 = off (default); N > 0 makes
+                                       the plain FP64 kernels of this handle wait N polls on a barrier
+                                       that nothing completes, so they end with UVATRMM_ETIMEOUT at the
+                                       next uvatrmm_sync (the context stays usable) */
+  UVATRMM_OPT_OZAKI_ERR_HOST = 11   /* 1: uvatrmm_ozaki_dtrmm_device's relerr_out is measured against
+                                       the host FP64 reference (A and the samples copied to the host),
+                                       as uvatrmm_ozaki_dtrmm's always is; 0 (default): against the
+                                       plain FP64 kernel on the device */
 } uvatrmm_option;
 typedef enum { UVATRMM_ENGINE_DFMA = 0, UVATRMM_ENGINE_DMMA = 1 } uvatrmm_engine;
 /* DYNAMIC: persistent CTAs pull tiles in longest-first order.
@@ -148,9 +156,11 @@ UVATRMM_API int uvatrmm_dtrmm_device_oop(uvatrmm_handle_t handle, int layout, in
  * lives in one fixed 64 MiB device array, so it rejects, with
  * UVATRMM_EINVAL and a message, problems whose staged B (round_up(rows, 16)
  * x cols doubles of the column-major view) plus any staged A exceed it.
- * A device holds the array from the first call there until the process
- * exits; that first call also looks up the array's device address and
- * should come before any stream capture.  All calls on a device share the
+ * A device reserves the array when the library's device code is loaded
+ * there (the first call on that device under CUDA's default lazy module
+ * loading; context creation under CUDA_MODULE_LOADING=EAGER) and holds it
+ * until the process exits.  The first call on a device also looks up the
+ * array's device address and should come before any stream capture.  All calls on a device share the
  * array: calls whose work overlaps on the GPU race.  Ordered on `stream` (a
  * cudaStream_t, NULL = legacy default stream); returns after the result is
  * in dB, with the kernel's status.  Plain DFMA engine, dynamic schedule. */
@@ -215,10 +225,15 @@ UVATRMM_API int uvatrmm_bc_scatter(uvatrmm_handle_t handle, int64_t m, int64_t n
  * residue slices; 0 = automatic, 2..20).  Same arguments and in-place
  * semantics as uvatrmm_dtrmm_device / uvatrmm_dtrmm; there is no reference
  * counterpart (the reference runs FP64 MKL only).  When relerr_out is not
- * NULL it receives the relative Frobenius error of the result against the
- * plain FP64 kernel over 8 evenly spaced result columns (side Left) or rows
- * (side Right), and the call synchronises.  *bits_out (if not NULL) receives
- * the bits kept per scaled operand entry. */
+ * NULL it receives the relative Frobenius error of the result over 8 evenly
+ * spaced result columns (side Left) or rows (side Right), and the call
+ * synchronises.  The reference for that error is FP64 arithmetic on the
+ * host: every sampled entry a compensated (Dot2) dot product of op(A) with
+ * the sampled input, computed on the host cores from the caller's own A and
+ * B for uvatrmm_ozaki_dtrmm, and for uvatrmm_ozaki_dtrmm_device from host
+ * copies when UVATRMM_OPT_OZAKI_ERR_HOST is 1 (else from the plain FP64
+ * kernel on the device).  *bits_out (if not NULL) receives the bits kept per
+ * scaled operand entry. */
 UVATRMM_API int uvatrmm_ozaki_dtrmm_device(uvatrmm_handle_t handle, int layout, int side, int uplo, int transa,
                                           int diag, int64_t m, int64_t n, double alpha, const double *dA,
                                           int64_t lda, double *dB, int64_t ldb, int moduli, double *relerr_out,
@@ -309,6 +324,9 @@ UVATRMM_API int uvatrmm_server_wait(uvatrmm_server_t server, int64_t id, double 
 /* Withdraws a request that has not been admitted yet. */
 UVATRMM_API int uvatrmm_server_cancel(uvatrmm_server_t server, int64_t id);
 UVATRMM_API int uvatrmm_server_get_stats(uvatrmm_server_t server, uvatrmm_server_stats *stats);
+/* Latency of completed request `id` in ms (submit -> result ready);
+ * UVATRMM_ENOTREADY while it is in flight, its error if it failed. */
+UVATRMM_API int uvatrmm_server_latency(uvatrmm_server_t server, int64_t id, double *ms);
 /* Finishes every queued request, then stops the server thread. */
 UVATRMM_API int uvatrmm_server_destroy(uvatrmm_server_t server);
 
@@ -355,13 +373,6 @@ UVATRMM_API int uvatrmm_gen_uniform(uvatrmm_handle_t handle, uint64_t seed, uint
 /* ||C||_inf of a row-major rows x cols device matrix (max row sum of |C|). */
 UVATRMM_API int uvatrmm_inf_norm(uvatrmm_handle_t handle, int64_t rows, int64_t cols, const double *dC,
                                  int64_t ldc, double *norm);
-
-/* ---------------------------------------------------------------- measurement */
-/* Measured FP64 peak of this device in TFLOP/s for one engine
- * (UVATRMM_ENGINE_DFMA: FMA on the CUDA cores; UVATRMM_ENGINE_DMMA: m8n8k4
- * FP64 tensor-core MMA), from a fixed in-register workload (~30 ms).  The
- * roofline denominator of the plain path. */
-UVATRMM_API int uvatrmm_probe_fp64_peak(uvatrmm_handle_t handle, int engine, double *tflops);
 
 /* ---------------------------------------------------------------- memory */
 /* Device memory and copies for C callers that do not include CUDA headers.

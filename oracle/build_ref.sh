@@ -9,11 +9,13 @@
 # Flags follow UVaTRMM/Makefile:13-14 (-O3 -fopenmp -std=c99 -DMININUMS=1).
 # MPI is replaced by the single-rank stub oracle/shim/mpi.h and MKL by
 # oracle/shim/mkl.h over the OpenBLAS that scipy bundles.
-# Usage: oracle/build_ref.sh [REFERENCE_ROOT]   (exits 0 and builds nothing
-# when the reference tree is absent).
+# Usage: oracle/build_ref.sh [REFERENCE_ROOT]
+# REFERENCE_ROOT is the argument, else $UVATRMM_REFERENCE_ROOT, else a
+# checkout named `reference` beside this repository's directory.  Exits 0 and
+# builds nothing when the reference tree is absent.
 set -euo pipefail
 HERE="$(cd "$(dirname "$0")" && pwd)"
-REF="${1:-/root/reference}"
+REF="${1:-${UVATRMM_REFERENCE_ROOT:-$HERE/../../reference}}"
 SRC="$REF/UVaTRMM"
 if [ ! -d "$SRC/src" ]; then
   echo "build_ref: reference sources not found at $SRC; skipping" >&2

@@ -60,3 +60,32 @@ def view(buf, layout, rows, cols, ld):
 def rel_fro(x, ref):
     d = np.linalg.norm(ref)
     return np.linalg.norm(x - ref) / (d if d > 0 else 1.0)
+
+
+def oracle_result(p):
+    """The oracle's logical m x n result for a problem dict (layout, side, uplo,
+    transa, diag, m, n, alpha, A (host array or CUDA tensor), lda, B0 (the host
+    input buffer), ldb, tier) and the tolerance of its tier: FP64 against the
+    naive FP64 loops at 8 k eps, Ozaki against the double-double oracle at
+    1e-14 (relative Frobenius)."""
+    A = p["A"].cpu().numpy() if hasattr(p["A"], "cpu") else p["A"]
+    layout, m, n = p["layout"], p["m"], p["n"]
+    args = (layout, p["side"], p["uplo"], p["transa"], p["diag"], m, n, p["alpha"])
+    if p.get("tier", 0) == 1:
+        R = orc.dtrmm_dd(*args, A, p["lda"], p["B0"].copy(), p["ldb"])
+        return (R if layout == COL else R.T), 1e-14
+    ref = p["B0"].copy()
+    orc.dtrmm_naive(*args, A, p["lda"], ref, p["ldb"])
+    k = m if p["side"] == LEFT else n
+    return view(ref, layout, m, n, p["ldb"]), 8 * max(k, 1) * EPS
+
+
+def assert_matches_oracle(p, got_buf, what=""):
+    """Asserts that the flat result buffer of problem p is within its tier's
+    tolerance of the oracle (see oracle_result)."""
+    if p["m"] == 0 or p["n"] == 0:
+        return
+    ref, tol = oracle_result(p)
+    got = view(got_buf, p["layout"], p["m"], p["n"], p["ldb"])
+    err = rel_fro(got, ref)
+    assert err <= tol, (what, p.get("tier"), p["m"], p["n"], err, tol)

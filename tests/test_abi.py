@@ -91,3 +91,15 @@ def test_ozaki_plan_is_monotonic(built):
     assert bits >= 52 and 14 <= auto <= 20
     with pytest.raises(u.UvatrmmError):
         u.ozaki_plan(100, 1)
+
+
+def test_noalloc_refuses_oversized_problems_without_touching_the_device(built):
+    """The no-allocation entry point bounds every dimension before it
+    multiplies sizes out: problems whose scratch would exceed the fixed array
+    (including sizes whose byte counts overflow 64 bits) are refused with
+    UVATRMM_EINVAL before any CUDA call, so this runs without a GPU."""
+    L = u.lib()
+    for (m, n) in ((4096, 4096), (1 << 40, 1 << 40), (16, 1 << 60), (1 << 61, 4)):
+        rc = L.uvatrmm_dtrmm_device_noalloc(102, 141, 122, 111, 131, m, n, 1.0, 16, m, 16, m, None)
+        assert rc == u.EINVAL, (m, n)
+        assert b"no-allocation" in L.uvatrmm_last_error()

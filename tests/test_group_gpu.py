@@ -1,14 +1,19 @@
 """Grouped batches (one CUDA graph of grouped persistent launches) against
 the single-problem entry points: bitwise identical results, because every
 output element accumulates in the same order (FP64 tier) or exactly (Ozaki
-tier) however the problems are grouped."""
+tier) however the problems are grouped.  Every grouped result is also
+checked against the oracle: FP64-tier results against the naive FP64 loops
+at 8 k eps, Ozaki-tier results against the double-double oracle at 1e-14
+(cblas_dtrmm semantics, as the reference calls it at
+UVaTRMM/src/mm_triangular.c:374-387)."""
 import os
 
 import numpy as np
 import pytest
 
 import uvatrmm_gb300 as u
-from tests.helpers import COL, LEFT, LOWER, NONUNIT, NOTRANS, RIGHT, ROW, TRANS, UNIT, UPPER, make_problem
+from tests.helpers import (COL, LEFT, LOWER, NONUNIT, NOTRANS, RIGHT, ROW, TRANS, UNIT, UPPER, assert_matches_oracle,
+                           make_problem)
 
 pytestmark = pytest.mark.gpu
 
@@ -65,7 +70,10 @@ def test_group_matches_single_calls_bitwise(handle):
         g.run()
         handle.sync()
         for p, r in zip(probs, refs):
-            assert np.array_equal(p["B"].cpu().numpy(), r), (rep, p["tier"], p["m"], p["n"])
+            got = p["B"].cpu().numpy()
+            assert np.array_equal(got, r), (rep, p["tier"], p["m"], p["n"])
+            if rep == 0:
+                assert_matches_oracle(p, got, "grouped")
         zb = probs[-1]["B"].cpu().numpy()
         m, n, ldb, layout = z["m"], z["n"], z["ldb"], z["layout"]
         rows, cols = (m, n) if layout == COL else (n, m)
@@ -87,7 +95,9 @@ def test_group_ozaki_waves_under_a_small_budget(handle):
     g.run()
     handle.sync()
     for p, r in zip(probs, refs):
-        assert np.array_equal(p["B"].cpu().numpy(), r)
+        got = p["B"].cpu().numpy()
+        assert np.array_equal(got, r)
+        assert_matches_oracle(p, got, "grouped, several waves")
     g.close()
 
 

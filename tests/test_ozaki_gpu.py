@@ -174,3 +174,66 @@ def test_ozaki_zero_rows_and_alpha_zero(handle):
     got = B.copy()
     handle.ozaki(COL, LEFT, LOWER, NOTRANS, NONUNIT, m, n, 0.0, A, lda, got, ldb)
     assert np.all(got.reshape(n, ldb)[:, :m] == 0.0)
+
+
+def _sampled_relerr(layout, side, m, n, got, ldb, ref_cm, S=8):
+    """Relative Frobenius error over the error report's samples: S evenly
+    spaced columns (side Left of the column-major-normalised call) or rows
+    (side Right) of the result."""
+    M, N = ref_cm.shape
+    nside = side if layout == COL else (RIGHT if side == LEFT else LEFT)
+    g = np.lib.stride_tricks.as_strided(got, (M, N), (8, 8 * ldb))
+    cnt = N if nside == LEFT else M
+    S = min(S, cnt)
+    idx = [(cnt - 1) * s // (S - 1) if S > 1 else 0 for s in range(S)]
+    if nside == LEFT:
+        return rel_fro(g[:, idx], ref_cm[:, idx])
+    return rel_fro(g[idx, :], ref_cm[idx, :])
+
+
+@pytest.mark.parametrize("layout,side,uplo,trans,diag", [(COL, LEFT, LOWER, NOTRANS, UNIT),
+                                                         (ROW, RIGHT, UPPER, TRANS, NONUNIT),
+                                                         (COL, RIGHT, LOWER, NOTRANS, NONUNIT),
+                                                         (ROW, LEFT, UPPER, TRANS, UNIT),
+                                                         (COL, LEFT, UPPER, TRANS, NONUNIT),
+                                                         (COL, RIGHT, UPPER, TRANS, UNIT)])
+def test_error_report_against_the_host_fp64_reference(handle, layout, side, uplo, trans, diag):
+    """relerr_out of the host entry point is measured against FP64 on the host
+    (compensated dot products from the caller's own A and B).  With 6 moduli
+    the emulated result is deliberately coarse (about 21 bits), so the report
+    must equal the error against the double-double oracle over the same
+    sampled vectors; the device entry point with UVATRMM_OPT_OZAKI_ERR_HOST
+    reports the same number."""
+    import torch
+    m, n = 70, 45
+    A, lda, B, ldb = make_problem(layout, side, uplo, m, n, lda_pad=1, ldb_pad=2, seed=31)
+    ref_cm = orc.dtrmm_dd(layout, side, uplo, trans, diag, m, n, 1.5, A, lda, B, ldb)
+    got = B.copy()
+    err, bits = handle.ozaki(layout, side, uplo, trans, diag, m, n, 1.5, A, lda, got, ldb, moduli=6, want_err=True)
+    expect = _sampled_relerr(layout, side, m, n, got, ldb, ref_cm)
+    assert 1e-9 < expect < 1e-3, expect
+    assert abs(err - expect) <= 1e-6 * expect, (err, expect)
+    h = u.Handle()
+    try:
+        h.set_option("ozaki_err_host", 1)
+        dA = torch.from_numpy(A).cuda()
+        dB = torch.from_numpy(B.copy()).cuda()
+        derr, _ = h.ozaki_device(layout, side, uplo, trans, diag, m, n, 1.5, dA, lda, dB, ldb, moduli=6,
+                                 want_err=True)
+        assert np.array_equal(dB.cpu().numpy(), got)
+        assert derr == err
+    finally:
+        h.close()
+
+
+def test_error_report_is_zero_for_exact_products(handle):
+    """Integer operands give an exact emulated product and an exact host
+    reference (every partial sum is an integer below 2^53): the report is 0."""
+    rng = np.random.default_rng(5)
+    K, n = 700, 33
+    Af = rng.integers(-1024, 1025, size=(K, K)).astype(np.float64)
+    Bf = rng.integers(-1024, 1025, size=(K, n)).astype(np.float64)
+    A = np.asfortranarray(Af).ravel(order="F").copy()
+    B = np.asfortranarray(Bf).ravel(order="F").copy()
+    err, _ = handle.ozaki(COL, LEFT, UPPER, TRANS, NONUNIT, K, n, 1.0, A, K, B, K, want_err=True)
+    assert err == 0.0

@@ -223,3 +223,63 @@ def test_large_sampled_columns(handle, side, uplo, trans):
         orc.blas_dtrmm(COL, side, uplo, trans, NONUNIT, 8, n, 1.0, A, m, Bs, 8)
         ref, got = Bs.reshape(n, 8).T, C[sel, :]
     assert rel_fro(got, ref) <= 8 * m * EPS
+
+
+@pytest.mark.parametrize("schedule,shape", [(u.SCHED_BALANCED, u.SHAPE_BOXES), (u.SCHED_REG, u.SHAPE_TRAPEZOID),
+                                            (u.SCHED_DYNAMIC, u.SHAPE_TRAPEZOID)])
+def test_skinny_16384x256_sampled_columns(handle, schedule, shape):
+    """The skinny case of the plain-path configuration (m = 16384, n = 256,
+    uplo U) under the reference's balanced / reg row mappings and both message
+    shapes, the mapped product of UVaTRMM/src/mm_triangular.c:88-99,319-410;
+    eight sampled columns against OpenBLAS cblas_dtrmm."""
+    import torch
+    m, n = 16384, 256
+    dA = torch.empty(m * m, dtype=torch.float64, device="cuda")
+    dB = torch.empty(m * n, dtype=torch.float64, device="cuda")
+    handle.gen_uniform(1, 0, m, m, dA, 1, m, tri="U", fill=float("nan"))  # NaN in the unreferenced triangle
+    handle.gen_uniform(1, 1, m, n, dB, 1, m)
+    dC = torch.empty_like(dB)
+    handle.set_option("schedule", schedule)
+    handle.set_option("shape", shape)
+    try:
+        handle.dtrmm_device_oop(COL, LEFT, UPPER, NOTRANS, NONUNIT, m, n, 1.0, dA, m, dB, m, dC, m)
+        handle.sync()
+    finally:
+        handle.set_option("schedule", u.SCHED_DYNAMIC)
+        handle.set_option("shape", u.SHAPE_TRAPEZOID)
+    A = dA.cpu().numpy()
+    sel = [0, 1, 77, 128, 129, 200, 254, 255]
+    Bs = np.concatenate([dB[j * m:(j + 1) * m].cpu().numpy() for j in sel])
+    orc.blas_dtrmm(COL, LEFT, UPPER, NOTRANS, NONUNIT, m, len(sel), 1.0, A, m, Bs, m)
+    got = np.concatenate([dC[j * m:(j + 1) * m].cpu().numpy() for j in sel])
+    assert rel_fro(got, Bs) <= 8 * m * EPS
+
+
+def test_wait_expiry_reports_etimeout_and_the_handle_recovers(handle):
+    """The kernel's bounded waits: with the test option set, the consumers wait
+    on a barrier that nothing completes, give up after the set number of
+    polls, record the timeout flag and return (the producer drains its copies
+    in flight first).  The host reads UVATRMM_ETIMEOUT at the next sync; the
+    same handle then computes the next call correctly."""
+    import torch
+    h = u.Handle()
+    try:
+        m, n = 1024, 512
+        A, lda, B, ldb = make_problem(COL, LEFT, LOWER, m, n, seed=5)
+        dA = torch_dev(A)
+        ref = oracle_result(COL, LEFT, LOWER, NOTRANS, NONUNIT, m, n, 1.0, A, lda, B, ldb)
+        for engine in (u.ENGINE_DFMA, u.ENGINE_DMMA):
+            h.set_option("engine", engine)
+            h.set_option("wait_expiry_test", 1000)
+            dB = torch_dev(B.copy())
+            h.dtrmm_device(COL, LEFT, LOWER, NOTRANS, NONUNIT, m, n, 1.0, dA, lda, dB, ldb)
+            with pytest.raises(u.UvatrmmError) as ei:
+                h.sync()
+            assert ei.value.status == u.ETIMEOUT
+            h.set_option("wait_expiry_test", 0)
+            dB = torch_dev(B.copy())
+            h.dtrmm_device(COL, LEFT, LOWER, NOTRANS, NONUNIT, m, n, 1.0, dA, lda, dB, ldb)
+            h.sync()
+            check_close(dB.cpu().numpy(), ref, B, m)
+    finally:
+        h.close()

@@ -10,8 +10,8 @@ import numpy as np
 import pytest
 
 import uvatrmm_gb300 as u
-from tests.helpers import (COL, EPS, LEFT, LOWER, NONUNIT, NOTRANS, RIGHT, ROW, TRANS, UNIT, UPPER, make_problem,
-                           rel_fro)
+from tests.helpers import (COL, EPS, LEFT, LOWER, NONUNIT, NOTRANS, RIGHT, ROW, TRANS, UNIT, UPPER,
+                           assert_matches_oracle, make_problem, rel_fro)
 
 pytestmark = pytest.mark.gpu
 
@@ -41,6 +41,9 @@ def test_noalloc_matches_allocating_entry_point(handle):
             assert np.array_equal(g[pad], B[pad])
             k = m if side == LEFT else n
             assert rel_fro(g[~pad], r[~pad]) <= 8 * k * EPS
+            # and against the oracle (naive FP64 cblas_dtrmm loops), same tolerance
+            assert_matches_oracle(dict(layout=layout, side=side, uplo=uplo, transa=trans, diag=diag, m=m, n=n,
+                                       alpha=-1.5, A=A, lda=lda, B0=B, ldb=ldb, tier=u.TIER_FP64), g, "no-alloc")
 
 
 def test_noalloc_rejects_problems_beyond_its_scratch(handle):
@@ -52,3 +55,10 @@ def test_noalloc_rejects_problems_beyond_its_scratch(handle):
                                         d.data_ptr(), m, None)
     assert rc == u.EINVAL
     assert b"no-allocation" in L.uvatrmm_last_error()
+    # sizes whose scratch products would overflow 64-bit arithmetic are refused
+    # too, before any device memory is touched
+    for (mm, nn) in ((1 << 40, 1 << 40), (16, 1 << 60), (1 << 61, 4)):
+        rc = L.uvatrmm_dtrmm_device_noalloc(COL, LEFT, LOWER, NOTRANS, NONUNIT, mm, nn, 1.0, d.data_ptr(), mm,
+                                            d.data_ptr(), mm, None)
+        assert rc == u.EINVAL, (mm, nn)
+        assert b"no-allocation" in L.uvatrmm_last_error()

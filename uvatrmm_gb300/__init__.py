@@ -63,7 +63,7 @@ class Handle:
     def set_option(self, name: str, value: int) -> None:
         key = {"engine": OPT_ENGINE, "schedule": OPT_SCHEDULE, "shape": OPT_SHAPE, "tile": OPT_TILE,
                "ozaki_scratch_mb": 5, "stage_timing": 6, "autotune": 7, "ozaki_raster": 8,
-               "host_stage_kb": 9}[name]
+               "host_stage_kb": 9, "wait_expiry_test": 10, "ozaki_err_host": 11}[name]
         check(lib().uvatrmm_set_option(self.h, key, int(value)))
 
     def stage_times(self):
@@ -143,11 +143,6 @@ class Handle:
         secs = C.c_double()
         check(lib().uvatrmm_product(self.h, n, schedule, shape, _ptr(dA), _ptr(dB), _ptr(dC), C.byref(secs)))
         return secs.value
-
-    def probe_fp64_peak(self, engine) -> float:
-        v = C.c_double()
-        check(lib().uvatrmm_probe_fp64_peak(self.h, engine, C.byref(v)))
-        return v.value
 
     # -- generators and norms -------------------------------------------------
     def gen_consecutive(self, n, triangular, d) -> None:
@@ -235,6 +230,11 @@ class Server:
 
     def cancel(self, rid: int) -> int:
         return lib().uvatrmm_server_cancel(self.s, rid)
+
+    def latency_ms(self, rid: int):
+        """Submit -> result-ready ms of a completed request (None while in flight or failed)."""
+        v = C.c_double()
+        return v.value if lib().uvatrmm_server_latency(self.s, rid, C.byref(v)) == 0 else None
 
     def stats(self) -> dict:
         from ._lib import ServerStats

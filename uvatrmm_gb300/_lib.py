@@ -41,7 +41,6 @@ SIGNATURES = {
     "uvatrmm_gen_consecutive": (i32, [vp, i64, i32, vp]),
     "uvatrmm_gen_uniform": (i32, [vp, u64, u64, i64, i64, vp, i64, i64, i32, dbl, i32]),
     "uvatrmm_inf_norm": (i32, [vp, i64, i64, vp, i64, C.POINTER(dbl)]),
-    "uvatrmm_probe_fp64_peak": (i32, [vp, i32, C.POINTER(dbl)]),
     "uvatrmm_device_alloc": (i32, [C.c_size_t, C.POINTER(vp)]),
     "uvatrmm_device_free": (i32, [vp]),
     "uvatrmm_copy": (i32, [vp, vp, vp, C.c_size_t, i32]),
@@ -79,6 +78,7 @@ SIGNATURES.update({
     "uvatrmm_server_wait": (i32, [vp, i64, dbl]),
     "uvatrmm_server_cancel": (i32, [vp, i64]),
     "uvatrmm_server_get_stats": (i32, [vp, C.POINTER(ServerStats)]),
+    "uvatrmm_server_latency": (i32, [vp, i64, C.POINTER(dbl)]),
     "uvatrmm_server_destroy": (i32, [vp]),
     "uvatrmm_group_create": (i32, [vp, C.POINTER(TrmmProblem), i32, C.POINTER(vp)]),
     "uvatrmm_group_run": (i32, [vp]),

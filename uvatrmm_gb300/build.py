@@ -28,7 +28,7 @@ CLI = os.path.join(BUILD, "uvatrmm.x")
 
 ARCH = ["-gencode", "arch=compute_103a,code=sm_103a"]
 NVFLAGS = ARCH + ["-lineinfo", "-O3", "-std=c++17", "--expt-relaxed-constexpr",
-                  "-Xcompiler", "-fPIC,-fvisibility=hidden", "-I", INCLUDE, "-I", CSRC]
+                  "-Xcompiler", "-fPIC,-fvisibility=hidden,-ffp-contract=off", "-I", INCLUDE, "-I", CSRC]
 
 
 def nvcc() -> str:

@@ -160,6 +160,7 @@ int run_fp64(uvatrmm_handle_t h, const Trmm &t, const double *A, int64_t lda, co
   L.counter = h->dctl;
   L.status = h->dctl + 1;
   L.num_sms = h->num_sms;
+  L.expiry_test_polls = h->expiry_test_polls;
   const char *why = nullptr;
   int rc = launch_trmm_fp64(L, h->stream, &why);
   if (rc != UVATRMM_OK) return fail(rc, why ? why : "kernel launch failed");
@@ -344,6 +345,14 @@ UVATRMM_API int uvatrmm_set_option(uvatrmm_handle_t h, int option, int value) {
     case UVATRMM_OPT_HOST_STAGE_KB:
       if (value != 0 && value < 64) break;
       h->hstage_bytes = (size_t)(value ? value : 262144) << 10;
+      return ok();
+    case UVATRMM_OPT_OZAKI_ERR_HOST:
+      if (value != 0 && value != 1) break;
+      h->oz_err_host = value != 0;
+      return ok();
+    case UVATRMM_OPT_WAIT_EXPIRY_TEST:
+      if (value < 0 || value > (int)kSpinLimit) break;
+      h->expiry_test_polls = (uint32_t)value;
       return ok();
     case UVATRMM_OPT_AUTOTUNE:
       if (value != 0 && value != 1) break;

@@ -20,6 +20,8 @@ struct uvatrmm_handle_st {
   int64_t ozaki_scratch_mb = 49152;  // residue-plane budget per pass (MiB)
   bool autotune = true;
   int oz_raster = 0;  // residue-GEMM raster group of single Ozaki calls (0 = default)
+  uint32_t expiry_test_polls = 0;  // UVATRMM_OPT_WAIT_EXPIRY_TEST (0 = off)
+  bool oz_err_host = false;        // UVATRMM_OPT_OZAKI_ERR_HOST
   // Grow-only device workspace slots: 0-2 plain-path and GEMM staging,
   // 3 reductions, 4 Ozaki scales, 5 Ozaki residue planes, 6 Ozaki product
   // residues, 7 Ozaki error-estimate scratch and the block-cyclic pointer
@@ -98,6 +100,13 @@ int device_trmm(uvatrmm_handle_t h, int layout, int side, int uplo, int transa, 
 int ozaki_device(uvatrmm_handle_t h, int layout, int side, int uplo, int transa, int diag, int64_t m, int64_t n,
                  double alpha, const double *dA, int64_t lda, double *dB, int64_t ldb, int moduli, double *relerr,
                  int *bits_out);
+
+// Relative Frobenius error of S sampled result vectors `got` against a
+// compensated FP64 host computation from op(A) (host memory, column-major
+// view of the normalised call) and the S sampled input vectors `b` (both
+// stored vector after vector, m entries each for side Left, n for side
+// Right); ozaki_err.cu.
+double host_ref_relerr(const Trmm &t, const double *A, int64_t lda, int S, const double *b, const double *got);
 
 // Autotuner (tune.cu): tuned tile edge (FP64) or raster group (Ozaki) for a
 // problem shape; measures and caches a missing bucket when h->autotune.

@@ -55,11 +55,11 @@ __device__ __forceinline__ bool mbar_try_wait(uint64_t *bar, uint32_t parity) {
   return ok != 0;
 }
 
-// Wait for phase `parity` of `bar` to complete, at most kSpinLimit polls.
+// Wait for phase `parity` of `bar` to complete, at most `limit` polls.
 // Returns false on timeout (the caller records KERR_WAIT_TIMEOUT and winds
 // down instead of hanging).
-__device__ __forceinline__ bool mbar_wait_bounded(uint64_t *bar, uint32_t parity) {
-  for (uint32_t it = 0; it < kSpinLimit; ++it)
+__device__ __forceinline__ bool mbar_wait_bounded(uint64_t *bar, uint32_t parity, uint32_t limit = kSpinLimit) {
+  for (uint32_t it = 0; it < limit; ++it)
     if (mbar_try_wait(bar, parity)) return true;
   return false;
 }

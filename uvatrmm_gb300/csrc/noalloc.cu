@@ -9,11 +9,13 @@
 // takes it from g_noalloc_scratch, a fixed file-scope device array, so a call
 // allocates nothing: no cudaMalloc, no cudaFree, no allocating library call.
 //
-// The array is part of this file's device module: every GPU on which the
-// entry point has run holds it until the process exits.  Its device address
-// is looked up once per device (cudaGetSymbolAddress, with that device
-// current) on the first call there; make that first call before any stream
-// capture.  All calls on a device share the array and it keeps the last
+// The array is part of this file's device module, so a GPU reserves it when
+// the library's device code is loaded there -- at the first call on that
+// device under CUDA's default lazy module loading, at context creation under
+// CUDA_MODULE_LOADING=EAGER -- and holds it until the process exits.  Its
+// device address is looked up once per device (cudaGetSymbolAddress, with
+// that device current) on the first call there; make that first call before
+// any stream capture.  All calls on a device share the array and it keeps the last
 // call's contents: the control words are cleared by each call, and calls
 // whose work overlaps on the GPU (different streams, or host threads without
 // ordering between them) race on it.
@@ -63,13 +65,18 @@ extern "C" UVATRMM_API int uvatrmm_dtrmm_device_noalloc(int layout, int side, in
   if (t.m == 0 || t.n == 0) return ok();
   const int64_t ka = t.side == CblasLeft ? t.m : t.n;
   const bool stage_a = (reinterpret_cast<uintptr_t>(dA) % 16 != 0) || (lda % 2 != 0);
-  const int64_t lb = round_up(t.m, 16), la = round_up(ka, 16);
-  const size_t b_bytes = (size_t)round_up(lb * t.n * 8, 256);
-  const size_t a_bytes = stage_a ? (size_t)la * ka * 8 : 0;
-  if (alpha != 0.0 && kNoAllocCtl + b_bytes + a_bytes > kNoAllocBytes)
-    return fail(UVATRMM_EINVAL, "no-allocation TRMM: the problem needs " +
-                                    std::to_string(kNoAllocCtl + b_bytes + a_bytes) +
-                                    " bytes of scratch, more than the fixed " + std::to_string(kNoAllocBytes) +
+  // Every dimension is bounded by a division before any size is multiplied
+  // out, so no product below can overflow.
+  const int64_t avail = (int64_t)(kNoAllocBytes - kNoAllocCtl);
+  bool fits = t.m <= avail / 8 && ka <= avail / 8;
+  const int64_t lb = fits ? round_up(t.m, 16) : 0, la = fits ? round_up(ka, 16) : 0;
+  fits = fits && t.n <= avail / (8 * lb) && (!stage_a || ka <= avail / (8 * la));
+  const size_t b_bytes = fits ? (size_t)round_up(lb * t.n * 8, 256) : 0;
+  const size_t a_bytes = fits && stage_a ? (size_t)la * ka * 8 : 0;
+  fits = fits && kNoAllocCtl + b_bytes + a_bytes <= kNoAllocBytes;
+  if (alpha != 0.0 && !fits)
+    return fail(UVATRMM_EINVAL, "no-allocation TRMM: the problem needs more scratch than the fixed " +
+                                    std::to_string(kNoAllocBytes) +
                                     " bytes (B staged as round_up(rows,16) x cols doubles, plus A when it is not "
                                     "16-byte aligned with an even leading dimension)");
   int dev = 0;

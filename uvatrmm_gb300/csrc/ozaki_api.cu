@@ -1,7 +1,10 @@
 // C ABI of the Ozaki-style emulated FP64 TRMM (see ozaki.cuh for the method).
 #include <algorithm>
 #include <cstring>
+#include <memory>
+#include <new>
 #include <string>
+#include <vector>
 
 #include "api_internal.h"
 #include "common.cuh"
@@ -25,6 +28,37 @@ void operands(const Trmm &t, const double *dA, int64_t lda, const double *dB, in
     L = OzOperand{dB, ldb, t.m, t.n, false, false, false, false, false};
     R = OzOperand{dA, lda, t.n, t.n, t.trans == 0, true, false, lower, t.unit != 0};
   }
+}
+
+// Sample positions of the error report: S evenly spaced result columns
+// (side Left) or rows (side Right) out of `cnt`.
+int64_t sample_index(int S, int s, int64_t cnt) { return S > 1 ? (cnt - 1) * s / (S - 1) : 0; }
+
+// Copies the S sampled vectors of the column-major matrix X (leading
+// dimension ld; host memory, or device memory when `device`) into `out`,
+// vector after vector.
+int gather_samples(uvatrmm_handle_t h, const Trmm &t, int S, const double *X, int64_t ld, bool device,
+                   double *out) {
+  const bool left = t.side == CblasLeft;
+  const int64_t len = left ? t.m : t.n, cnt = left ? t.n : t.m;
+  for (int s = 0; s < S; ++s) {
+    const int64_t idx = sample_index(S, s, cnt);
+    double *o = out + (int64_t)s * len;
+    if (device) {
+      cudaError_t e = left ? cudaMemcpyAsync(o, X + idx * ld, len * 8, cudaMemcpyDeviceToHost, h->stream)
+                           : cudaMemcpy2DAsync(o, 8, X + idx, ld * 8, 8, len, cudaMemcpyDeviceToHost, h->stream);
+      if (e != cudaSuccess) return cuda_fail(e, "error-report sample");
+    } else if (left) {
+      std::memcpy(o, X + idx * ld, (size_t)len * 8);
+    } else {
+      for (int64_t k = 0; k < len; ++k) o[k] = X[idx + k * ld];
+    }
+  }
+  if (device) {
+    cudaError_t e = cudaStreamSynchronize(h->stream);
+    if (e != cudaSuccess) return cuda_fail(e, "error-report sample");
+  }
+  return UVATRMM_OK;
 }
 
 }  // namespace
@@ -201,8 +235,34 @@ UVATRMM_API int uvatrmm_ozaki_dtrmm_device(uvatrmm_handle_t h, int layout, int s
                                           double *dB, int64_t ldb, int moduli, double *relerr_out, int *bits_out) {
   if (!(h = resolve(h))) return uvatrmm_last_status();
   std::lock_guard<std::mutex> g(h->mu);
-  return ozaki_device(h, layout, side, uplo, transa, diag, m, n, alpha, dA, lda, dB, ldb, moduli, relerr_out,
-                      bits_out);
+  if (!relerr_out || !h->oz_err_host)
+    return ozaki_device(h, layout, side, uplo, transa, diag, m, n, alpha, dA, lda, dB, ldb, moduli, relerr_out,
+                        bits_out);
+  // Error against the host FP64 reference: the sampled inputs and op(A) are
+  // copied to the host around the call.
+  if (int bad = check_args(layout, side, uplo, transa, diag, m, n, lda, ldb))
+    return fail(UVATRMM_EINVAL, "parameter " + std::to_string(bad) + " had an illegal value");
+  const Trmm t = normalise(layout, side, uplo, transa, diag, m, n, alpha);
+  *relerr_out = 0.0;
+  const bool left = t.side == CblasLeft;
+  const int64_t len = left ? t.m : t.n, cnt = left ? t.n : t.m, ka = len;
+  const int S = (int)std::min<int64_t>(kErrSamples, cnt);
+  std::vector<double> b((size_t)S * len), got((size_t)S * len);
+  std::unique_ptr<double[]> A;  // host copy of A (not zero-filled: every entry read is copied in)
+  if (S && alpha != 0.0) {
+    if (int rc = gather_samples(h, t, S, dB, ldb, true, b.data())) return rc;
+    A.reset(new (std::nothrow) double[(size_t)ka * ka]);
+    if (!A) return fail(UVATRMM_ENOMEM, "host memory for the error report's copy of A");
+    cudaError_t e = cudaMemcpy2DAsync(A.get(), ka * 8, dA, lda * 8, ka * 8, ka, cudaMemcpyDeviceToHost, h->stream);
+    if (e != cudaSuccess) return cuda_fail(e, "error-report copy of A");
+  }
+  int rc = ozaki_device(h, layout, side, uplo, transa, diag, m, n, alpha, dA, lda, dB, ldb, moduli, nullptr,
+                        bits_out);
+  if (rc != UVATRMM_OK || !S || alpha == 0.0) return rc;
+  if ((rc = collect_status(h)) != UVATRMM_OK) return rc;
+  if ((rc = gather_samples(h, t, S, dB, ldb, true, got.data())) != UVATRMM_OK) return rc;
+  *relerr_out = host_ref_relerr(t, A.get(), ka, S, b.data(), got.data());
+  return ok();
 }
 
 UVATRMM_API int uvatrmm_ozaki_dtrmm(uvatrmm_handle_t h, int layout, int side, int uplo, int transa, int diag,
@@ -222,14 +282,27 @@ UVATRMM_API int uvatrmm_ozaki_dtrmm(uvatrmm_handle_t h, int layout, int side, in
   cudaError_t e = host_copy2d(h, dA, la * 8, A, lda * 8, ka * 8, ka, cudaMemcpyHostToDevice);
   if (e == cudaSuccess) e = host_copy2d(h, dB, lb * 8, B, ldb * 8, t.m * 8, t.n, cudaMemcpyHostToDevice);
   if (e != cudaSuccess) return cuda_fail(e, "host to device copy");
+  // Error report: the sampled inputs are kept before B is overwritten; the
+  // reference is computed on the host from the caller's own A and B.
+  const bool left = t.side == CblasLeft;
+  const int64_t len = left ? t.m : t.n, cnt = left ? t.n : t.m;
+  const int S = relerr_out && alpha != 0.0 ? (int)std::min<int64_t>(kErrSamples, cnt) : 0;
+  if (relerr_out) *relerr_out = 0.0;
+  std::vector<double> bs((size_t)S * len), got((size_t)S * len);
+  if (S) gather_samples(h, t, S, B, ldb, false, bs.data());
   int rc = ozaki_device(h, CblasColMajor, t.side, t.uplo, t.trans ? CblasTrans : CblasNoTrans,
-                        t.unit ? CblasUnit : CblasNonUnit, t.m, t.n, t.alpha, dA, la, dB, lb, moduli, relerr_out,
+                        t.unit ? CblasUnit : CblasNonUnit, t.m, t.n, t.alpha, dA, la, dB, lb, moduli, nullptr,
                         bits_out);
   if (rc != UVATRMM_OK) return rc;
   e = host_copy2d(h, B, ldb * 8, dB, lb * 8, t.m * 8, t.n, cudaMemcpyDeviceToHost);
   if (e != cudaSuccess) return cuda_fail(e, "device to host copy");
   rc = collect_status(h);
-  return rc == UVATRMM_OK ? ok() : rc;
+  if (rc != UVATRMM_OK) return rc;
+  if (S) {
+    gather_samples(h, t, S, B, ldb, false, got.data());
+    *relerr_out = host_ref_relerr(t, A, lda, S, bs.data(), got.data());
+  }
+  return ok();
 }
 
 }  // extern "C"

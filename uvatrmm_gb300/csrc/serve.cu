@@ -710,6 +710,17 @@ UVATRMM_API int uvatrmm_server_cancel(uvatrmm_server_t s, int64_t id) {
   return ok();
 }
 
+UVATRMM_API int uvatrmm_server_latency(uvatrmm_server_t s, int64_t id, double *ms) {
+  if (!s || !ms) return fail(UVATRMM_EINVAL, "invalid arguments");
+  std::lock_guard<std::mutex> lk(s->mu);
+  auto it = s->reqs.find(id);
+  if (it == s->reqs.end()) return fail(UVATRMM_EINVAL, "unknown request id");
+  const Req &r = *it->second;
+  if (r.state != DONE) return fail(r.state == FAILED ? r.status : UVATRMM_ENOTREADY, "request not completed");
+  *ms = (r.t_done - r.t_submit) * 1e3;
+  return ok();
+}
+
 UVATRMM_API int uvatrmm_server_get_stats(uvatrmm_server_t s, uvatrmm_server_stats *out) {
   if (!s || !out) return fail(UVATRMM_EINVAL, "invalid arguments");
   std::lock_guard<std::mutex> lk(s->mu);

@@ -55,6 +55,8 @@ struct StageInfo {
 
 struct KParams : TileProb {
   int *counter, *status;
+  uint32_t spin;    // poll limit of the waits on work (kSpinLimit unless testing expiry)
+  int expiry_test;  // consumers first wait on a barrier that nothing completes
   int sched_static, Q, CP;
   int qb[kMaxBlocks + 1];  // work-rank bounds of the Q major blocks
   int cb[kMaxBlocks + 1];  // bounds of the CP minor panels
@@ -73,7 +75,10 @@ struct Cfg {
   static constexpr int L_ELEMS = BM * kBK, R_ELEMS = BN * kBK;
   static constexpr uint32_t STAGE_BYTES = (L_ELEMS + R_ELEMS) * 8u;
   static constexpr int MIN_BLOCKS = BM == 128 ? 1 : 2;
-  static constexpr size_t SMEM = 1024 + STAGES * (size_t)STAGE_BYTES + STAGES * 16 + STAGES * sizeof(StageInfo);
+  // Ring, full/empty barriers, stage records, and one barrier that only the
+  // expiry test waits on.
+  static constexpr size_t SMEM =
+      1024 + STAGES * (size_t)STAGE_BYTES + STAGES * 16 + STAGES * sizeof(StageInfo) + 16;
 };
 
 // Slab element readers.  K-major slabs were written by TMA with the 128-byte
@@ -324,6 +329,7 @@ __global__ void __launch_bounds__(Cfg<BM>::THREADS, Cfg<BM>::MIN_BLOCKS)
   uint64_t *full = reinterpret_cast<uint64_t *>(base + C::STAGES * C::STAGE_BYTES);
   uint64_t *empty = full + C::STAGES;
   StageInfo *info = reinterpret_cast<StageInfo *>(empty + C::STAGES);
+  uint64_t *never = reinterpret_cast<uint64_t *>(info + C::STAGES);  // nothing arrives on it
   auto Lst = [&](int s) { return reinterpret_cast<double *>(base + s * C::STAGE_BYTES); };
   auto Rst = [&](int s) { return reinterpret_cast<double *>(base + s * C::STAGE_BYTES) + C::L_ELEMS; };
 
@@ -333,6 +339,7 @@ __global__ void __launch_bounds__(Cfg<BM>::THREADS, Cfg<BM>::MIN_BLOCKS)
       mbar_init(&full[s], 1);
       mbar_init(&empty[s], C::NCW);
     }
+    mbar_init(never, 1);
     fence_barrier_init();
   }
   __syncthreads();
@@ -348,7 +355,7 @@ __global__ void __launch_bounds__(Cfg<BM>::THREADS, Cfg<BM>::MIN_BLOCKS)
       uint32_t issued = 0;
       uint32_t last_ph[C::STAGES];
       auto claim = [&]() -> bool {  // wait until stage s is free
-        if (!mbar_wait_bounded(&empty[s], ph ^ 1)) {
+        if (!mbar_wait_bounded(&empty[s], ph ^ 1, p.spin)) {
           record_error(p.status, KERR_WAIT_TIMEOUT);
           return false;
         }
@@ -412,8 +419,13 @@ __global__ void __launch_bounds__(Cfg<BM>::THREADS, Cfg<BM>::MIN_BLOCKS)
     eng.init(threadIdx.x);
     int s = 0;
     uint32_t ph = 0;
-    while (true) {
-      if (!mbar_wait_bounded(&full[s], ph)) {
+    bool go = true;
+    if (p.expiry_test && !mbar_wait_bounded(never, 0, p.spin)) {
+      record_error(p.status, KERR_WAIT_TIMEOUT);
+      go = false;
+    }
+    while (go) {
+      if (!mbar_wait_bounded(&full[s], ph, p.spin)) {
         record_error(p.status, KERR_WAIT_TIMEOUT);
         break;
       }
@@ -468,6 +480,7 @@ __global__ void __launch_bounds__(Cfg<BM>::THREADS, Cfg<BM>::MIN_BLOCKS)
   uint64_t *full = reinterpret_cast<uint64_t *>(base + C::STAGES * C::STAGE_BYTES);
   uint64_t *empty = full + C::STAGES;
   StageInfo *info = reinterpret_cast<StageInfo *>(empty + C::STAGES);
+  uint64_t *never = reinterpret_cast<uint64_t *>(info + C::STAGES);  // nothing arrives on it
   auto Lst = [&](int s) { return reinterpret_cast<double *>(base + s * C::STAGE_BYTES); };
   auto Rst = [&](int s) { return reinterpret_cast<double *>(base + s * C::STAGE_BYTES) + C::L_ELEMS; };
 
@@ -477,6 +490,7 @@ __global__ void __launch_bounds__(Cfg<BM>::THREADS, Cfg<BM>::MIN_BLOCKS)
       mbar_init(&full[s], 1);
       mbar_init(&empty[s], C::NCW);
     }
+    mbar_init(never, 1);
     fence_barrier_init();
   }
   __syncthreads();
@@ -697,6 +711,8 @@ int launch_trmm_fp64(const Fp64Launch &L, cudaStream_t stream, const char **why)
   memset(&kp, 0, sizeof(kp));
   kp.M = L.M; kp.N = L.N; kp.K = L.K; kp.ldc = L.ldc;
   kp.alpha = L.alpha; kp.beta = L.beta; kp.C = L.C; kp.counter = L.counter; kp.status = L.status;
+  kp.spin = L.expiry_test_polls ? L.expiry_test_polls : kSpinLimit;
+  kp.expiry_test = L.expiry_test_polls != 0;
   kp.tri_left = L.tri_left; kp.tri_lower = L.tri_lower; kp.unit = L.unit;
   kp.tri_none = L.tri_none;
   kp.trapezoid = L.shape == UVATRMM_SHAPE_TRAPEZOID;

@@ -39,6 +39,11 @@ struct Fp64Launch {
   int num_sms;
   double beta = 0.0;     // C = alpha*op*B + beta*C (0: C is only written)
   bool tri_none = false;  // plain GEMM: neither operand triangular
+  // Tests of the failure path only (0 = off): the consumers first wait, with
+  // this many polls, on a barrier that nothing completes, and every wait on
+  // work uses the same limit, so the launch ends with KERR_WAIT_TIMEOUT; the
+  // producer's final drain of its copies in flight keeps the default limit.
+  uint32_t expiry_test_polls = 0;
 };
 
 // Enqueues the kernel on `stream`.  Returns a uvatrmm_status.
