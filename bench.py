@@ -841,7 +841,8 @@ def run_ozaki(args, h, dev, stream, rank, plain_tflops):
     moduli, bits = u.ozaki_plan(m)
 
     def step(mo=0, want_err=False):
-        dB.copy_(dB0)
+        with torch.cuda.stream(stream):  # ordered before the library's work on the same stream
+            dB.copy_(dB0)
         ev0, ev1 = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
         ev0.record(stream)
         err, b = h.ozaki_device(C_, Le, Up, Tr, NU, m, n, 1.0, dA, m, dB, m, moduli=mo, want_err=want_err)

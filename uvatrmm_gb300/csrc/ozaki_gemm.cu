@@ -1,41 +1,49 @@
 // Exact residue GEMM on the 5th-generation tensor cores (tcgen05, sm_103a).
 //
-// For every modulus m_l and output tile (128 x 256 per CTA): the K loop runs
-// over 64-wide bf16 slabs staged by TMA (128-byte swizzle, K-major) into a
+// For every modulus m_l and output block of 256 x 256 the K loop runs over
+// 64-wide bf16 slabs staged by TMA (128-byte swizzle, K-major) into a
 // 4-stage shared-memory ring; one thread issues tcgen05.mma.kind::f16
-// (bf16 x bf16 -> fp32 in TMEM, M=128 N=256 K=16).  Every 8 slabs (a K chunk
-// of 512) the accumulator is handed to the epilogue warps, which reduce it
-// modulo m_l in place (tcgen05.ld -> fp32 fold -> tcgen05.st) while the MMA
-// thread fills the other TMEM accumulator with the next chunk; the next chunk
-// for that accumulator then adds on top of the folded value.  Residues are
-// at most 181 in magnitude (moduli up to 363) and a folded value at most a
-// few units past m/2, so every value the accumulator ever holds is an
+// (bf16 x bf16 -> fp32 in TMEM, K=16 per instruction).  Every 8 slabs (a K
+// chunk of 512) the accumulator is handed to the epilogue warps, which reduce
+// it modulo m_l in place (tcgen05.ld -> fp32 fold -> tcgen05.st) while the
+// MMA thread fills the other TMEM accumulator with the next chunk; the next
+// chunk for that accumulator then adds on top of the folded value.  Residues
+// are at most 181 in magnitude (moduli up to 363) and a folded value at most
+// a few units past m/2, so every value the accumulator ever holds is an
 // integer below 512 * 181^2 + 184 < 2^24 and fp32 accumulation is exact.
 // The last two chunks are combined and the tile's residues r are written as
 // the 16-bit words u_l r mod m_l (u_l = (M/m_l)^-1 mod m_l, for the CRT).
 //
-// CTA pairs.  The kernel runs in clusters of two CTAs stacked along M: the
-// pair computes a 256 x 256 block (rows 2*tp*128 + rank*128 for each CTA)
-// over one K range, the union of both row tiles' ranges (the extra slabs of
-// the shorter range only meet zeros of the triangle).  Each CTA loads its own
-// A tile and half of the shared B tile, which TMA multicasts into both CTAs'
-// shared memory, so every B byte leaves L2 once per pair.  A stage is free
-// again when both CTAs' MMAs have read it: each MMA thread's commit arrives
-// on the stage's empty barrier in both CTAs.
+// CTA pairs and the 2-SM MMA.  The kernel runs in clusters of two CTAs on
+// two SMs.  The pair computes a 256 x 256 block with tcgen05.mma.cta_group::2
+// (M = 256, N = 256): each CTA stages its own 128 rows of A and its own half
+// (128 rows) of the B tile in its own shared memory, and the MMA, issued by
+// one thread of the even CTA (the leader), reads A and B from both CTAs and
+// accumulates each CTA's 128 rows in that CTA's TMEM.  Per 16-wide K step an
+// SM thus stages and reads 8 KB of operands for 128 x 256 outputs, where a
+// single-CTA M = 128 MMA over the whole B tile needs 12 KB -- shared-memory
+// bandwidth is what bounds this GEMM.  Both CTAs' copies complete on the
+// leader's "full" barrier (the .cta_group::2 form of the TMA load); the
+// leader's commits free the stage in both CTAs ("empty") and hand each
+// finished chunk to both CTAs' epilogues ("cdone"), whose warps release the
+// accumulator on the leader's "afree" barrier.  No load is multicast: every
+// copy lands in the shared memory of the CTA that issued it.  The pair's K
+// range is the union of its two row tiles' ranges (the extra slabs of the
+// shorter range only meet zeros of the triangle).
 //
-// The accumulators alternate across tiles (chunk g of a CTA uses buffer
+// The accumulators alternate across tiles (chunk g of a pair uses buffer
 // g & 1).  The second-to-last chunk of a tile is reduced to residues (low
 // bytes in shared memory, the ninth bits in a per-thread word per 32
 // columns) and its buffer released at once, so the next tile's first chunk
 // runs while the last chunk is combined and stored.
 //
 // Warp roles (320 threads, one CTA per SM): warp 0 TMA producer, warp 1 TMEM
-// owner + MMA issuer, warps 2-9 epilogue (each bound to its TMEM lane
-// quadrant, warp % 4, and to half of the columns).  Tiles go to clusters
-// round-robin in a raster of pair-row groups (see decode()).  All mbarrier
-// waits are bounded; on expiry the kernel
-// records KERR_WAIT_TIMEOUT, drains its copies and MMAs, frees TMEM and exits
-// (after the pair's closing cluster barrier).
+// owner (both CTAs allocate the pair's columns together) and, in the leader,
+// MMA issuer; warps 2-9 epilogue (each bound to its TMEM lane quadrant,
+// warp % 4, and to half of the columns).  Tiles go to clusters round-robin
+// in a raster of pair-row groups (see decode()).  All mbarrier waits are
+// bounded; on expiry the kernel records KERR_WAIT_TIMEOUT, drains its copies
+// and MMAs, frees TMEM and exits (after the pair's closing cluster barrier).
 #include <algorithm>
 #include <cstring>
 
@@ -47,14 +55,14 @@ namespace uvt {
 namespace {
 
 constexpr int BM = 128, BN = 256, BK = 64;
-constexpr int PAIR = 2;          // CTAs per cluster, stacked along M
+constexpr int PAIR = 2;          // CTAs per cluster, stacked along M; one 2-SM MMA per K step
 static_assert(PAIR * BM == kOzBlock && BN == kOzBlock, "the slicing skips tiles by this K-range geometry");
-constexpr int BH = BN / PAIR;    // rows of the B tile each CTA loads and multicasts
-constexpr uint16_t PAIR_MASK = (1u << PAIR) - 1;
+constexpr int BH = BN / PAIR;    // rows of the B tile each CTA stages (its half of N)
 constexpr int STAGES = 4;
 constexpr int CHUNK_SLABS = 8;  // K chunk of 512 between modular folds
-constexpr uint32_t A_BYTES = BM * BK * 2, B_BYTES = BN * BK * 2, BH_BYTES = BH * BK * 2;
-constexpr uint32_t STAGE_BYTES = A_BYTES + B_BYTES;
+constexpr uint32_t A_BYTES = BM * BK * 2, BH_BYTES = BH * BK * 2;
+constexpr uint32_t STAGE_BYTES = A_BYTES + BH_BYTES;  // one CTA's share of a stage
+constexpr uint32_t PAIR_TX = PAIR * STAGE_BYTES;      // bytes landing on the leader's full barrier
 // Warp 0: TMA producer; warp 1: MMA issuer; warps 2..9: epilogue, two warps
 // per TMEM lane quarter (warp & 3), each taking half of the 256 columns, so a
 // tile's last-chunk epilogue stays within one chunk of MMAs.
@@ -66,8 +74,10 @@ constexpr uint32_t TMEM_COLS = 2 * BN;  // two fp32 accumulators of 256 columns
 constexpr uint32_t R1_BYTES = BM * BN;
 constexpr size_t SMEM = 1024 + (size_t)STAGES * STAGE_BYTES + 256 + R1_BYTES;
 // kind::f16 instruction descriptor: D fp32 (bits 4-5 = 1), A and B bf16
-// (bits 7-9 = 1, 10-12 = 1), both K-major, N/8 at bits 17-22, M/16 at 24-28.
-constexpr uint32_t IDESC = (1u << 4) | (1u << 7) | (1u << 10) | ((uint32_t)(BN >> 3) << 17) | ((uint32_t)(BM >> 4) << 24);
+// (bits 7-9 = 1, 10-12 = 1), both K-major, N/8 at bits 17-22, M/16 at 24-28
+// with M = 256, the pair's rows.
+constexpr uint32_t IDESC =
+    (1u << 4) | (1u << 7) | (1u << 10) | ((uint32_t)(BN >> 3) << 17) | ((uint32_t)((PAIR * BM) >> 4) << 24);
 
 // Launch-wide parameters; the problems themselves are OzGroupProb entries in
 // global memory (their tensor maps are read by TMA from there).
@@ -157,15 +167,31 @@ __device__ __forceinline__ void cluster_sync() {
   asm volatile("barrier.cluster.arrive.release.aligned;\n\tbarrier.cluster.wait.acquire.aligned;" ::: "memory");
 }
 
-// 2-D TMA load multicast to the same shared-memory offset (and the same
-// mbarrier offset) in every CTA of `mask`.
-__device__ __forceinline__ void tma_load_2d_mc(void *smem_dst, const CUtensorMap *m, int x, int y, uint64_t *bar,
-                                               uint16_t mask) {
+// Address of the same shared-memory location in CTA `rank` of the cluster.
+__device__ __forceinline__ uint32_t mapa(uint32_t saddr, uint32_t rank) {
+  uint32_t r;
+  asm volatile("mapa.shared::cluster.u32 %0, %1, %2;" : "=r"(r) : "r"(saddr), "r"(rank));
+  return r;
+}
+
+// 2-D TMA load into this CTA's shared memory whose completion is counted on
+// the mbarrier at cluster address `bar` (this CTA's or its pair peer's: the
+// .cta_group::2 form).
+__device__ __forceinline__ void tma_load_2d_pair(void *smem_dst, const CUtensorMap *m, int x, int y, uint32_t bar) {
   asm volatile(
-      "cp.async.bulk.tensor.2d.shared::cluster.global.mbarrier::complete_tx::bytes.multicast::cluster"
-      " [%0], [%1, {%2, %3}], [%4], %5;" ::"r"(smem_u32(smem_dst)),
-      "l"(reinterpret_cast<uint64_t>(m)), "r"(x), "r"(y), "r"(smem_u32(bar)), "h"(mask)
+      "cp.async.bulk.tensor.2d.cta_group::2.shared::cluster.global.mbarrier::complete_tx::bytes"
+      " [%0], [%1, {%2, %3}], [%4];" ::"r"(smem_u32(smem_dst)),
+      "l"(reinterpret_cast<uint64_t>(m)), "r"(x), "r"(y), "r"(bar)
       : "memory");
+}
+
+// Arrive on the mbarrier at cluster address `bar` (this CTA's or the pair
+// peer's).  The default semantics (release at CTA scope) suffice: what the
+// arrive hands over is TMEM, ordered by tcgen05.wait + tcgen05.fence around
+// it, not ordinary memory, so it need not wait for the warp's earlier global
+// stores to become visible across the cluster.
+__device__ __forceinline__ void mbar_arrive_remote(uint32_t bar) {
+  asm volatile("mbarrier.arrive.shared::cluster.b64 _, [%0];" ::"r"(bar) : "memory");
 }
 
 // ---------------------------------------------------------------- packed fp32 fold
@@ -197,26 +223,20 @@ __device__ __forceinline__ uint64_t sw128_desc(uint32_t saddr) {
   return d;
 }
 
-__device__ __forceinline__ void umma_bf16(uint32_t d_tmem, uint64_t a, uint64_t b, uint32_t acc) {
+// One 2-SM MMA: D[256 x 256] (+)= A[256 x 16] * B[16 x 256]^T, A's rows and
+// B's columns split between the pair's shared memories at the same offsets.
+__device__ __forceinline__ void umma_bf16_pair(uint32_t d_tmem, uint64_t a, uint64_t b, uint32_t acc) {
   asm volatile(
       "{\n .reg .pred p;\n setp.ne.b32 p, %4, 0;\n"
-      " tcgen05.mma.cta_group::1.kind::f16 [%0], %1, %2, %3, p;\n}\n" ::"r"(d_tmem),
+      " tcgen05.mma.cta_group::2.kind::f16 [%0], %1, %2, %3, p;\n}\n" ::"r"(d_tmem),
       "l"(a), "l"(b), "r"(IDESC), "r"(acc)
       : "memory");
 }
 
-__device__ __forceinline__ void umma_commit(uint64_t *bar) {
-  asm volatile("tcgen05.commit.cta_group::1.mbarrier::arrive::one.shared::cluster.b64 [%0];" ::"r"(smem_u32(bar))
-               : "memory");
-}
-
-// Commit whose arrive lands on the barrier at the same offset in every CTA of `mask`.
-__device__ __forceinline__ void umma_commit_mc(uint64_t *bar, uint16_t mask) {
-  asm volatile(
-      "tcgen05.commit.cta_group::1.mbarrier::arrive::one.shared::cluster.multicast::cluster.b64 [%0], %1;" ::"r"(
-          smem_u32(bar)),
-      "h"(mask)
-      : "memory");
+// Arrive-once on the mbarrier at cluster address `bar` when this thread's
+// earlier 2-SM MMAs have completed.
+__device__ __forceinline__ void umma_commit_pair(uint32_t bar) {
+  asm volatile("tcgen05.commit.cta_group::2.mbarrier::arrive::one.shared::cluster.b64 [%0];" ::"r"(bar) : "memory");
 }
 
 __device__ __forceinline__ void tc_fence_before() { asm volatile("tcgen05.fence::before_thread_sync;" ::: "memory"); }
@@ -272,23 +292,25 @@ __global__ void __cluster_dims__(PAIR, 1, 1) __launch_bounds__(NUM_THREADS, 1)
 
   const int warp = threadIdx.x >> 5, lane = threadIdx.x & 31;
   const uint32_t rank = cluster_rank();
+  const bool leader = rank == 0;  // issues the pair's MMAs; its barriers pace the pair
   if (threadIdx.x == 0) {
     for (int s = 0; s < STAGES; ++s) {
-      mbar_init(&full[s], 1);
-      mbar_init(&empty[s], PAIR);  // one commit from each CTA's MMA thread
+      mbar_init(&full[s], 1);   // leader: its expect_tx arrival, then both CTAs' bytes
+      mbar_init(&empty[s], 1);  // the leader's commit after the stage's MMAs
     }
     for (int b = 0; b < 2; ++b) {
-      mbar_init(&cdone[b], 1);
-      mbar_init(&afree[b], EPI_WARPS);
+      mbar_init(&cdone[b], 1);                 // the leader's commit at a chunk's end
+      mbar_init(&afree[b], PAIR * EPI_WARPS);  // leader: every epilogue warp of the pair
     }
     mbar_init(drain, 1);
     fence_barrier_init();
   }
   if (warp == 1) {
-    asm volatile("tcgen05.alloc.cta_group::1.sync.aligned.shared::cta.b32 [%0], %1;" ::"r"(smem_u32(tmem_slot)),
+    // The pair allocates its accumulator columns together (one warp of each CTA).
+    asm volatile("tcgen05.alloc.cta_group::2.sync.aligned.shared::cta.b32 [%0], %1;" ::"r"(smem_u32(tmem_slot)),
                  "r"(TMEM_COLS)
                  : "memory");
-    asm volatile("tcgen05.relinquish_alloc_permit.cta_group::1.sync.aligned;" ::: "memory");
+    asm volatile("tcgen05.relinquish_alloc_permit.cta_group::2.sync.aligned;" ::: "memory");
     tc_fence_before();
   }
   // Both CTAs' barriers are initialised before either CTA's copies or
@@ -321,25 +343,35 @@ __global__ void __cluster_dims__(PAIR, 1, 1) __launch_bounds__(NUM_THREADS, 1)
             ok = false;
             break;
           }
-          // This CTA's A tile, its half of B for both CTAs, the peer's half of B: STAGE_BYTES.
-          mbar_arrive_expect_tx(&full[s], STAGE_BYTES);
-          tma_load_2d(smA(s), &P.tmA, ks * BK, ya, &full[s]);
-          tma_load_2d_mc(smB(s) + rank * BH_BYTES, &P.tmB, ks * BK, yb, &full[s], PAIR_MASK);
+          // This CTA's A tile and its half of B, both counted on the leader's
+          // full barrier, which expects both CTAs' bytes.
+          const uint32_t fb = mapa(smem_u32(&full[s]), 0);
+          if (leader) mbar_arrive_expect_tx(&full[s], PAIR_TX);
+          tma_load_2d_pair(smA(s), &P.tmA, ks * BK, ya, fb);
+          tma_load_2d_pair(smB(s), &P.tmB, ks * BK, yb, fb);
           issued |= 1u << s;
           last_ph[s] = ph;
           if (++s == STAGES) { s = 0; ph ^= 1; }
         }
       }
+      // Drain.  The leader's full barriers count both CTAs' copies, so once
+      // its last phases have completed nothing is in flight into either CTA.
+      // The peer cannot see that barrier; it waits instead until the
+      // leader's MMAs have released every stage it filled (which they do
+      // only after its copies landed), so it never leaves with a copy in
+      // flight into its own shared memory.
       for (int st = 0; st < STAGES; ++st)
         if ((issued >> st) & 1u)
-          if (!mbar_wait_bounded(&full[st], last_ph[st])) record_error(p.status, KERR_WAIT_TIMEOUT);
+          if (!mbar_wait_bounded(leader ? &full[st] : &empty[st], last_ph[st]))
+            record_error(p.status, KERR_WAIT_TIMEOUT);
     }
   } else if (warp == 1) {
-    // ------------------------------------------------------------ MMA issuer
-    if (lane == 0) {
+    // ------------------------------------------------------------ MMA issuer (leader)
+    if (lane == 0 && leader) {
       int s = 0;
       uint32_t ph = 0, gc = 0;
       bool ok = true, any = false;
+      const uint32_t peer = rank ^ 1u;
       for (int t = (int)cluster_index(); ok && t < p.total_tiles; t += (int)cluster_count()) {
         const OzGroupProb &P = probs[find_problem(probs, p.nprob, t)];
         const Tile T = decode(P, t - P.tile_begin + P.tile_offset, (int)cluster_count());
@@ -366,19 +398,22 @@ __global__ void __cluster_dims__(PAIR, 1, 1) __launch_bounds__(NUM_THREADS, 1)
 #pragma unroll
             for (int kk = 0; kk < BK / 16; ++kk) {
               const uint32_t acc = (c >= 2 || sl > sl0 || kk > 0) ? 1u : 0u;
-              umma_bf16(d_tmem, sw128_desc(a0 + kk * 32), sw128_desc(b0 + kk * 32), acc);
+              umma_bf16_pair(d_tmem, sw128_desc(a0 + kk * 32), sw128_desc(b0 + kk * 32), acc);
             }
-            umma_commit_mc(&empty[s], PAIR_MASK);  // frees stage s in both CTAs once read
+            // Stage s is free in both CTAs once these MMAs have read it.
+            umma_commit_pair(smem_u32(&empty[s]));
+            umma_commit_pair(mapa(smem_u32(&empty[s]), peer));
             any = true;
             if (++s == STAGES) { s = 0; ph ^= 1; }
           }
           if (!ok) break;
-          umma_commit(&cdone[b]);
+          umma_commit_pair(smem_u32(&cdone[b]));
+          umma_commit_pair(mapa(smem_u32(&cdone[b]), peer));
         }
       }
       // Drain: all MMAs this thread issued complete before TMEM is freed.
       if (any) {
-        umma_commit(drain);
+        umma_commit_pair(smem_u32(drain));
         if (!mbar_wait_bounded(drain, 0)) record_error(p.status, KERR_WAIT_TIMEOUT);
       }
     }
@@ -475,17 +510,19 @@ __global__ void __cluster_dims__(PAIR, 1, 1) __launch_bounds__(NUM_THREADS, 1)
         }
         tc_fence_before();
         __syncwarp();
-        if (lane == 0) mbar_arrive(&afree[b]);
+        // The accumulator is free once every epilogue warp of the pair has
+        // arrived on the leader's barrier.
+        if (lane == 0) mbar_arrive_remote(mapa(smem_u32(&afree[b]), 0));
       }
     }
   }
   __syncthreads();
-  // Neither CTA leaves while the other may still multicast into its shared
-  // memory or arrive on its barriers.
+  // Neither CTA leaves while the other may still read its shared memory
+  // through the pair's MMAs or arrive on its barriers.
   cluster_sync();
   if (warp == 1) {
     tc_fence_after();
-    asm volatile("tcgen05.dealloc.cta_group::1.sync.aligned.b32 %0, %1;" ::"r"(tmem_base), "r"(TMEM_COLS)
+    asm volatile("tcgen05.dealloc.cta_group::2.sync.aligned.b32 %0, %1;" ::"r"(tmem_base), "r"(TMEM_COLS)
                  : "memory");
   }
 }
@@ -530,10 +567,10 @@ int oz_group_prob(const OzGemmLaunch &L, OzGroupProb *out, const char **why) {
   out->tiles_n = (int)(L.Np / BN);
   out->tiles_per_mod = (out->tiles_m / PAIR) * out->tiles_n;
   out->tile_count = out->tiles_per_mod * nmod;
-  // Default raster group (measured at m = n = 1024 .. 32768): 4 pair rows once
-  // both tile counts reach 64 (m, n >= 16384), 2 below.
-  const bool big = out->tiles_m / PAIR >= 64 && out->tiles_n >= 64;
-  out->group = L.raster_group > 0 ? L.raster_group : (big ? 4 : 2);
+  // Default raster group (measured with the 2-SM MMA at m = n = 4096 .. 32768):
+  // 3 pair rows once both tile counts reach 32 (m, n >= 8192), 2 below.
+  const bool big = out->tiles_m / PAIR >= 32 && out->tiles_n >= 32;
+  out->group = L.raster_group > 0 ? L.raster_group : (big ? 3 : 2);
   out->res = L.res;
   out->plane = L.Mp * L.Np;
   out->nmod = L.n_moduli;

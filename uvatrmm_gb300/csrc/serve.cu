@@ -361,15 +361,39 @@ bool launch_tick(uvatrmm_server_t s, std::vector<Req *> &act) {
   for (Req *r : oldest)
     if (r) order.push_back(r);
   order.insert(order.end(), rest.begin(), rest.end());
-  for (Req *r : order) {
+  // Tiles per request: first the shares above; then the tick is made
+  // work-conserving -- budget nobody else could use goes to the requests in
+  // the same order (the oldest first), so a request running with little
+  // company is not held to a quarter of the device.
+  std::vector<int> takes(order.size(), 0);
+  int n_oz = 0, n_f64 = 0;
+  for (size_t i = 0; i < order.size(); ++i) {
+    Req *r = order[i];
     const bool oz = r->p.tier == UVATRMM_TIER_OZAKI;
     double &budget = oz ? o_budget : f_budget;
     if (budget <= 0) continue;
+    if ((oz ? n_oz : n_f64) >= s->cfg.max_active) continue;
     const double share = r == oldest[oz ? 1 : 0] ? 0.25 * (oz ? s->cfg.tick_ozaki_gflop : s->cfg.tick_fp64_gflop) * 1e9
                                                  : budget;
-    int take = (int)std::min<double>(r->total - r->next, std::max(1.0, std::ceil(share / r->tile_cost)));
-    if ((int)(oz ? odesc.size() : fdesc.size()) >= s->cfg.max_active) continue;
+    const int take = (int)std::min<double>(r->total - r->next, std::max(1.0, std::ceil(share / r->tile_cost)));
     budget -= take * r->tile_cost;
+    takes[i] = take;
+    (oz ? n_oz : n_f64)++;
+  }
+  for (size_t i = 0; i < order.size(); ++i) {
+    Req *r = order[i];
+    if (!takes[i]) continue;
+    double &budget = r->p.tier == UVATRMM_TIER_OZAKI ? o_budget : f_budget;
+    const int more = (int)std::min<double>(r->total - r->next - takes[i], std::floor(budget / r->tile_cost));
+    if (more <= 0) continue;
+    takes[i] += more;
+    budget -= more * r->tile_cost;
+  }
+  for (size_t i = 0; i < order.size(); ++i) {
+    Req *r = order[i];
+    const int take = takes[i];
+    if (!take) continue;
+    const bool oz = r->p.tier == UVATRMM_TIER_OZAKI;
     if (oz) {
       if (!r->prepped) {
         prep.push_back(r);
