@@ -44,10 +44,14 @@ sys.path.insert(0, ROOT)
 METRIC = "TRMM TFLOP/s, FP64 DMMA vs Ozaki at <=1e-14 rel err; served p50/p99 latency"
 NOMINAL_FP64_TFLOPS = 1.25
 FP64_FLOP_PER_CLK_SM = 4.0
-# DRAM bytes per flop of the FP64 kernel measured by ncu at m = n = 4096
-# (1.2965e9 B over 4096^3 flops); B panels are re-read per row tile.
-TRAFFIC_BYTES_PER_FLOP = 1.2965e9 / 4096.0 ** 3
-TRAFFIC_SOURCE = "ncu dram bytes per launch at m=n=4096, scaled by flops to this size"
+# DRAM bytes (read + write) per launch of the FP64 kernel measured by ncu on
+# smaller cases of the headline workload.  They grow faster than the flops
+# (x19.9 for x8 from 4096 to 8192: B panels are re-read per row tile and hit
+# L2 less as the operands grow), so they are not scaled to the bench size and
+# `traffic` is null there.
+TRAFFIC_MEASURED = {4096: 1.2965e9, 8192: 25.756e9}
+TRAFFIC_SOURCE = ("ncu dram__bytes_read.sum + dram__bytes_write.sum per launch at the sizes in traffic_measured; "
+                  "traffic grows faster than flops, so no figure is extrapolated to this size")
 
 
 def headline_config(m, n, ws):
@@ -328,7 +332,8 @@ def run_gpu(args, ws, rank, local):
                 "sync_step_ms": step_ms},
         "roofline": {"bound": "tensor", "achieved": round(achieved, 4), "peak": round(peak, 4), "unit": "TFLOP/s",
                      "frac": round(achieved / peak, 4),
-                     "traffic": TRAFFIC_BYTES_PER_FLOP * flops if m == n else None,
+                     "traffic": TRAFFIC_MEASURED.get(m) if m == n else None,
+                     "traffic_measured": {f"m=n={k}": v for k, v in TRAFFIC_MEASURED.items()},
                      "peak_source": f"FP64 issue limit {FP64_FLOP_PER_CLK_SM} flop/clk/SM x {n_sms} SMs x "
                                     f"{sm_mhz:.0f} MHz (sampled); MEASURED_PEAKS.json has no FP64 figure; "
                                     f"nominal GB300 FP64 {NOMINAL_FP64_TFLOPS}",
