@@ -114,7 +114,7 @@ def test_summary_closes_the_line():
                      "rel_fro_err_vs_dd_oracle": 2.2e-16, "library_relerr_vs_host_fp64": 2.1e-16,
                      "roofline": {"achieved": 1500.0, "frac": 0.88}, "clocks": {"sm_mhz": 1700, "reasons": []},
                      "slice_sweep": [{"int8_slices": 5, "moduli": 11, "bits": 37, "rel_fro_err_vs_dd_oracle": 1e-9}]},
-           "serving": {"max_steady_rate_req_per_s": 150.0, "alone_p99_ms": 139.0,
+           "serving": {"max_steady_rate_req_per_s": 150.0, "max_rate_p99_within_2x_alone": 50.0, "alone_p99_ms": 139.0,
                        "rates": [{"rate_req_per_s": 50.0, "p50_ms": 1.0, "p99_ms": 100.0, "p99_first_half_ms": 90.0,
                                   "p99_second_half_ms": 95.0, "sustained_tflops": 1.2}]},
            "cpu_baseline": {"value": 0.5}}
@@ -125,7 +125,7 @@ def test_summary_closes_the_line():
     assert s["check"]["headline_rel_err"] == 1.23e-16
     assert s["check"]["variants_rel_err"] == {"L reg/boxes": 2e-16, "skinny": 3e-16, "large": 4e-16}
     assert s["ozaki"]["moduli"] == 15 and s["ozaki"]["int8_sweep"] == [[5, 11, 37, 1e-9]]
-    assert s["serving"]["max_steady_rate"] == 150.0
+    assert s["serving"]["max_steady_rate"] == 150.0 and s["serving"]["max_rate_p99_2x_alone"] == 50.0
     assert len(json.dumps(s)) < 1400
 
 
