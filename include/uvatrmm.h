@@ -93,7 +93,7 @@ typedef enum {
   UVATRMM_OPT_STAGE_TIMING = 6,     /* 1: time the stages of each Ozaki call (uvatrmm_stage_times) */
   UVATRMM_OPT_AUTOTUNE = 7,         /* 1 (default): measure untuned shape buckets; 0: defaults only */
   UVATRMM_OPT_OZAKI_RASTER = 8,     /* Ozaki residue GEMM of single calls: major tiles per raster
-                                       group (0 = default: 3 when m, n >= 8192, else 2; or 1..64) */
+                                       group (0 = default: 2; or 1..64) */
   UVATRMM_OPT_HOST_STAGE_KB = 9,    /* chunk of the host staging used for host operands outside
                                        uvatrmm_host_alloc memory, KiB (0 = default 262144; >= 64) */
   UVATRMM_OPT_WAIT_EXPIRY_TEST = 10,/* tests of the failure path only: 0 = off (default); N > 0 makes
@@ -332,7 +332,7 @@ UVATRMM_API int uvatrmm_server_destroy(uvatrmm_server_t server);
 
 /* ---------------------------------------------------------------- autotuner */
 /* The tuned choice for a problem shape: FP64 tier -> output tile edge (64 or
- * 128); Ozaki tier -> residue-GEMM raster group (2, 3 or 4).  Shapes are
+ * 128); Ozaki tier -> residue-GEMM raster group (1, 2 or 3).  Shapes are
  * bucketed by (tier, side, ceil(log2 m), ceil(log2 n)); a missing bucket is
  * measured on the device (when UVATRMM_OPT_AUTOTUNE is 1, the default) and
  * cached in the file named by $UVATRMM_TUNE_CACHE (default

@@ -102,7 +102,7 @@ def test_group_ozaki_waves_under_a_small_budget(handle):
 
 
 def test_autotuner_choices_and_cache(handle):
-    for tier, allowed in ((u.TIER_FP64, (64, 128)), (u.TIER_OZAKI, (2, 3, 4))):
+    for tier, allowed in ((u.TIER_FP64, (64, 128)), (u.TIER_OZAKI, (1, 2, 3))):
         for side in (LEFT, RIGHT):
             c = u.tune(handle, tier, side, 300, 700)
             assert c in allowed

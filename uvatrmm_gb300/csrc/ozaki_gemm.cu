@@ -1,10 +1,11 @@
 // Exact residue GEMM on the 5th-generation tensor cores (tcgen05, sm_103a).
 //
 // For every modulus m_l and output block of 256 x 256 the K loop runs over
-// 64-wide bf16 slabs staged by TMA (128-byte swizzle, K-major) into a
-// 4-stage shared-memory ring; one thread issues tcgen05.mma.kind::f16
-// (bf16 x bf16 -> fp32 in TMEM, K=16 per instruction).  Every 8 slabs (a K
-// chunk of 512) the accumulator is handed to the epilogue warps, which reduce
+// 128-deep bf16 slabs, each two 64-wide atoms staged by TMA (128-byte
+// swizzle, K-major), in a 3-stage shared-memory ring; one thread issues
+// tcgen05.mma.kind::f16 (bf16 x bf16 -> fp32 in TMEM, K=16 per instruction,
+// eight per slab).  Every 4 slabs (a K chunk of 512) the accumulator is handed
+// to the epilogue warps, which reduce
 // it modulo m_l in place (tcgen05.ld -> fp32 fold -> tcgen05.st) while the
 // MMA thread fills the other TMEM accumulator with the next chunk; the next
 // chunk for that accumulator then adds on top of the folded value.  Residues
@@ -21,8 +22,8 @@
 // one thread of the even CTA (the leader), reads A and B from both CTAs and
 // accumulates each CTA's 128 rows in that CTA's TMEM.  Per 16-wide K step an
 // SM thus stages and reads 8 KB of operands for 128 x 256 outputs, where a
-// single-CTA M = 128 MMA over the whole B tile needs 12 KB -- shared-memory
-// bandwidth is what bounds this GEMM.  Both CTAs' copies complete on the
+// single-CTA M = 128 MMA over the whole B tile needs 12 KB, and no copy needs
+// to be multicast to share B.  Both CTAs' copies complete on the
 // leader's "full" barrier (the .cta_group::2 form of the TMA load); the
 // leader's commits free the stage in both CTAs ("empty") and hand each
 // finished chunk to both CTAs' epilogues ("cdone"), whose warps release the
@@ -58,9 +59,15 @@ constexpr int BM = 128, BN = 256, BK = 64;
 constexpr int PAIR = 2;          // CTAs per cluster, stacked along M; one 2-SM MMA per K step
 static_assert(PAIR * BM == kOzBlock && BN == kOzBlock, "the slicing skips tiles by this K-range geometry");
 constexpr int BH = BN / PAIR;    // rows of the B tile each CTA stages (its half of N)
-constexpr int STAGES = 4;
-constexpr int CHUNK_SLABS = 8;  // K chunk of 512 between modular folds
-constexpr uint32_t A_BYTES = BM * BK * 2, BH_BYTES = BH * BK * 2;
+// Two 64-wide swizzle atoms per stage: per 128-deep slab the producer, the
+// MMA thread and the barriers hand off once for eight MMAs (measured 5-10 %
+// faster than 64-deep slabs in a 4-stage ring, bit-identical results).
+constexpr int ATOMS = 2;
+constexpr int SLAB = ATOMS * BK;         // K per stage
+constexpr int STAGES = 3;
+constexpr int CHUNK_SLABS = 512 / SLAB;  // K chunk of 512 between modular folds
+constexpr uint32_t ATOM_A = BM * BK * 2, ATOM_B = BH * BK * 2;
+constexpr uint32_t A_BYTES = ATOMS * ATOM_A, BH_BYTES = ATOMS * ATOM_B;
 constexpr uint32_t STAGE_BYTES = A_BYTES + BH_BYTES;  // one CTA's share of a stage
 constexpr uint32_t PAIR_TX = PAIR * STAGE_BYTES;      // bytes landing on the leader's full barrier
 // Warp 0: TMA producer; warp 1: MMA issuer; warps 2..9: epilogue, two warps
@@ -142,8 +149,8 @@ __device__ __forceinline__ Tile decode(const OzGroupProb &p, int t, int ncluster
     if (p.tri_lower) { kb = j0; ke = p.K; }
     else { kb = 0; ke = min(j0 + BN, p.K); }
   }
-  T.ks0 = (int)(kb / BK);
-  T.ks1 = (int)((ke + BK - 1) / BK);
+  T.ks0 = (int)(kb / SLAB);
+  T.ks1 = (int)((ke + SLAB - 1) / SLAB);
   return T;
 }
 
@@ -347,8 +354,11 @@ __global__ void __cluster_dims__(PAIR, 1, 1) __launch_bounds__(NUM_THREADS, 1)
           // full barrier, which expects both CTAs' bytes.
           const uint32_t fb = mapa(smem_u32(&full[s]), 0);
           if (leader) mbar_arrive_expect_tx(&full[s], PAIR_TX);
-          tma_load_2d_pair(smA(s), &P.tmA, ks * BK, ya, fb);
-          tma_load_2d_pair(smB(s), &P.tmB, ks * BK, yb, fb);
+#pragma unroll
+          for (int a = 0; a < ATOMS; ++a) {
+            tma_load_2d_pair(smA(s) + a * ATOM_A, &P.tmA, ks * SLAB + a * BK, ya, fb);
+            tma_load_2d_pair(smB(s) + a * ATOM_B, &P.tmB, ks * SLAB + a * BK, yb, fb);
+          }
           issued |= 1u << s;
           last_ph[s] = ph;
           if (++s == STAGES) { s = 0; ph ^= 1; }
@@ -396,9 +406,10 @@ __global__ void __cluster_dims__(PAIR, 1, 1) __launch_bounds__(NUM_THREADS, 1)
             tc_fence_after();
             const uint32_t a0 = smem_u32(smA(s)), b0 = smem_u32(smB(s));
 #pragma unroll
-            for (int kk = 0; kk < BK / 16; ++kk) {
+            for (int kk = 0; kk < SLAB / 16; ++kk) {
               const uint32_t acc = (c >= 2 || sl > sl0 || kk > 0) ? 1u : 0u;
-              umma_bf16_pair(d_tmem, sw128_desc(a0 + kk * 32), sw128_desc(b0 + kk * 32), acc);
+              const uint32_t a = (uint32_t)(kk / (BK / 16)), w = (uint32_t)(kk % (BK / 16));
+              umma_bf16_pair(d_tmem, sw128_desc(a0 + a * ATOM_A + w * 32), sw128_desc(b0 + a * ATOM_B + w * 32), acc);
             }
             // Stage s is free in both CTAs once these MMAs have read it.
             umma_commit_pair(smem_u32(&empty[s]));
@@ -567,10 +578,9 @@ int oz_group_prob(const OzGemmLaunch &L, OzGroupProb *out, const char **why) {
   out->tiles_n = (int)(L.Np / BN);
   out->tiles_per_mod = (out->tiles_m / PAIR) * out->tiles_n;
   out->tile_count = out->tiles_per_mod * nmod;
-  // Default raster group (measured with the 2-SM MMA at m = n = 4096 .. 32768):
-  // 3 pair rows once both tile counts reach 32 (m, n >= 8192), 2 below.
-  const bool big = out->tiles_m / PAIR >= 32 && out->tiles_n >= 32;
-  out->group = L.raster_group > 0 ? L.raster_group : (big ? 3 : 2);
+  // Default raster group: 2 pair rows (measured best with 128-deep slabs at
+  // m = n = 8192 .. 32768 against 3; 3 was best with 64-deep slabs).
+  out->group = L.raster_group > 0 ? L.raster_group : 2;
   out->res = L.res;
   out->plane = L.Mp * L.Np;
   out->nmod = L.n_moduli;

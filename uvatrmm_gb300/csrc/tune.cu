@@ -1,5 +1,5 @@
 // Autotuner: per shape bucket, the FP64 output tile edge (64 or 128) and the
-// Ozaki residue-GEMM raster group (2, 3 or 4), measured on the device and
+// Ozaki residue-GEMM raster group (1, 2 or 3), measured on the device and
 // cached in a small text file ("tier side log2m log2n choice" per line).
 #include <sys/stat.h>
 
@@ -120,7 +120,7 @@ int tune_choice(uvatrmm_handle_t h, int tier, int side, int64_t m, int64_t n, in
   }
   uvatrmm_gen_uniform(h, 99, 0, ka, ka, dA, 1, ka, 0, 0.0, 0);
   uvatrmm_gen_uniform(h, 99, 1, rm, rn, dB, 1, rm, 0, 0.0, 0);
-  const int cand_fp64[2] = {64, 128}, cand_oz[3] = {2, 3, 4};
+  const int cand_fp64[2] = {64, 128}, cand_oz[3] = {1, 2, 3};
   const int *cand = tier == UVATRMM_TIER_FP64 ? cand_fp64 : cand_oz;
   const int ncand = tier == UVATRMM_TIER_FP64 ? 2 : 3;
   float best = 1e30f;
