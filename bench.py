@@ -438,6 +438,15 @@ def run_serving(args, h, dev, stream):
         h.sync()
         alone_ms.append((time.perf_counter() - t0) * 1e3)
     alone_p99 = _pct(alone_ms, 99)
+    alone_tier = [reqs[i]["tier"] for i in range(len(alone_ms))]
+
+    def by_tier(lats, tiers):
+        """p50 / p99 per accuracy tier."""
+        out = {}
+        for t, name in ((u.TIER_FP64, "fp64"), (u.TIER_OZAKI, "ozaki")):
+            v = [x for x, k in zip(lats, tiers) if k == t]
+            out[name] = {"n": len(v), "p50_ms": _pct(v, 50), "p99_ms": _pct(v, 99)}
+        return out
     rates = []
     for rate in args.serve_rates:
         count = max(1, int(round(rate * args.serve_seconds)))
@@ -458,7 +467,9 @@ def run_serving(args, h, dev, stream):
             last[k] = srv.submit(reqs[k])
             ids.append(last[k])
         bad = sum(srv.wait(r) != 0 for r in ids)
-        lat = [x for x in (srv.latency_ms(r) for r in ids) if x is not None]
+        pairs = [(srv.latency_ms(r), reqs[i % len(reqs)]["tier"]) for i, r in enumerate(ids)]
+        lat = [x for x, _ in pairs if x is not None]
+        tiers = [t for x, t in pairs if x is not None]
         st = srv.stats()
         srv.close()
         span = st["last_done_s"] - st["first_submit_s"]
@@ -470,7 +481,7 @@ def run_serving(args, h, dev, stream):
                       "mean_ms": round(float(np.mean(lat)), 3) if lat else None, "max_ms": round(max(lat), 3),
                       "offered_tflops": round(served / (count / rate) / 1e12, 4),
                       "sustained_tflops": round(st["served_flops"] / span / 1e12, 4), "ticks": st["ticks"],
-                      "peak_pool_gib": round(st["peak_bytes"] / 2 ** 30, 2)})
+                      "peak_pool_gib": round(st["peak_bytes"] / 2 ** 30, 2), "by_tier": by_tier(lat, tiers)})
     # Highest rate served in steady state (no failures, the second half's p99
     # within 1.5x the first half's: the queue does not grow), and the highest
     # of those whose p99 also stays within 2x the one-at-a-time p99.
@@ -482,7 +493,7 @@ def run_serving(args, h, dev, stream):
                         "request operand sets, m logU[128,8192], n logU[32,8192], 50% FP64 / 50% Ozaki (<=1e-14), "
                         "side/uplo/trans uniform, 120 GB budget, device-resident operands, seed 4",
             "alone_p50_ms": _pct(alone_ms, 50), "alone_p99_ms": alone_p99,
-            "alone_requests": len(alone_ms),
+            "alone_requests": len(alone_ms), "alone_by_tier": by_tier(alone_ms, alone_tier),
             "alone_capacity_req_per_s": round(1e3 / float(np.mean(alone_ms)), 1),
             "mean_gflop_per_request": round(sum(flops) / len(flops) / 1e9, 2),
             "max_steady_rate_req_per_s": max((r["rate_req_per_s"] for r in steady), default=None),

@@ -237,3 +237,35 @@ def test_error_report_is_zero_for_exact_products(handle):
     B = np.asfortranarray(Bf).ravel(order="F").copy()
     err, _ = handle.ozaki(COL, LEFT, UPPER, TRANS, NONUNIT, K, n, 1.0, A, K, B, K, want_err=True)
     assert err == 0.0
+
+
+@pytest.mark.parametrize("side,uplo,trans", [(LEFT, UPPER, TRANS), (LEFT, LOWER, NOTRANS),
+                                             (RIGHT, LOWER, NOTRANS), (RIGHT, UPPER, TRANS)])
+def test_ozaki_large_wide_exponents_sampled_vs_double_double(handle, side, uplo, trans):
+    """m = n = 6144 on the device with entries uniform[-1,1) * 2^k, k in [-20, 20]
+    (the precision configuration's distribution) and NaN in the unreferenced
+    triangle: sampled result columns (side Left) or rows (side Right) within
+    1e-14 of the double-double oracle."""
+    import torch
+    m = n = 6144
+    ka = m
+    dA = torch.empty(ka * ka, dtype=torch.float64, device="cuda")
+    dB = torch.empty(m * n, dtype=torch.float64, device="cuda")
+    handle.gen_uniform(7, 0, ka, ka, dA, 1, ka, tri="L" if uplo == LOWER else "U", fill=float("nan"), spread=20)
+    handle.gen_uniform(7, 1, m, n, dB, 1, m, spread=20)
+    handle.sync()
+    A = dA.cpu().numpy()
+    B0 = dB.cpu().numpy()
+    handle.ozaki_device(COL, side, uplo, trans, NONUNIT, m, n, 1.0, dA, ka, dB, m)
+    handle.sync()
+    got_all = dB.cpu().numpy()
+    sel = [0, 1, 2047, 4096, 6143]
+    got, ref = [], []
+    for j in sel:
+        if side == LEFT:
+            ref.append(orc.dtrmm_dd(COL, side, uplo, trans, NONUNIT, m, n, 1.0, A, ka, B0, m, cols=(j, j + 1))[:, 0])
+            got.append(got_all[j * m:(j + 1) * m])
+        else:
+            ref.append(orc.dtrmm_dd(COL, side, uplo, trans, NONUNIT, m, n, 1.0, A, ka, B0, m, rows=(j, j + 1))[0, :])
+            got.append(got_all[j::m])
+    assert rel_fro(np.concatenate(got), np.concatenate(ref)) <= TOL
