@@ -7,13 +7,14 @@
 //            stream;
 //   tick   - one grouped launch per kind over tile ranges taken from every
 //            active request (Ozaki slicing of newly admitted requests, the
-//            residue GEMM, the FP64 TRMM, Ozaki reassembly of requests whose
-//            last GEMM tiles are in this tick), alternating between two
+//            residue GEMM, Ozaki reassembly of requests whose last GEMM tiles
+//            are in this tick, then the FP64 TRMM), alternating between two
 //            compute streams with two ticks in flight, so one tick's tail
 //            overlaps the next tick and the device never waits for the host;
-//   retire - when a tick's event completes, requests whose last work was in
-//            it are finished (host mode: after their result's copy back),
-//            their memory returns to the pool, and waiters are woken.
+//   retire - when a tick's Ozaki work completes, the Ozaki requests
+//            reassembled in it are finished; when the whole tick completes,
+//            its FP64 requests are (host mode: after their result's copy
+//            back); their memory returns to the pool and waiters are woken.
 #include <algorithm>
 #include <chrono>
 #include <condition_variable>
@@ -136,9 +137,13 @@ struct TickSlot {
   char *host = nullptr;  // pinned mirror
   cudaEvent_t done = nullptr;
   cudaEvent_t prepped = nullptr;  // this tick's Ozaki slicing finished
+  cudaEvent_t gemm_done = nullptr;  // this tick's residue GEMM (and slicing) finished
+  cudaEvent_t oz_done = nullptr;    // this tick's Ozaki work finished (before its FP64 launch)
   bool has_prep = false;
+  bool oz_retired = false;          // finishing_oz already retired
   int64_t id = -1;
-  std::vector<int64_t> finishing;  // requests whose last work is in this tick
+  std::vector<int64_t> finishing;     // FP64-tier requests whose last work is in this tick
+  std::vector<int64_t> finishing_oz;  // Ozaki-tier requests reassembled in this tick
 };
 
 }  // namespace
@@ -474,26 +479,34 @@ bool launch_tick(uvatrmm_server_t s, std::vector<Req *> &act) {
   if (rc == UVATRMM_OK && !odesc.empty())
     rc = launch_oz_gemm_group(reinterpret_cast<OzGroupProb *>(slot.dev + s->off_oz), (int)odesc.size(), o_begin,
                               s->h->dctl + 1, s->h->num_sms, cs, &why);
+  cudaEventRecord(slot.gemm_done, cs);
+  // The tick's Ozaki work comes before its FP64 tiles, so Ozaki requests that
+  // finish here retire on oz_done without waiting for those tiles.
+  if (rc == UVATRMM_OK && !reas.empty()) {
+    // Earlier residue tiles of these requests ran in previous ticks: the one
+    // before this (other stream) up to its residue GEMM; older ticks retired.
+    if (prev) cudaStreamWaitEvent(cs, prev->gemm_done, 0);
+    rc = oz_wave_reassemble(treas, cs);
+  }
+  cudaEventRecord(slot.oz_done, cs);
   if (rc == UVATRMM_OK && !fdesc.empty())
     rc = launch_trmm_fp64_group(reinterpret_cast<Fp64GroupProb *>(slot.dev + s->off_f64), (int)fdesc.size(),
                                 f_begin, 64, UVATRMM_ENGINE_DFMA, s->h->dctl + 2 + (int)(id % 2), s->h->dctl + 1,
                                 s->h->num_sms, cs, &why);
-  if (rc == UVATRMM_OK && !reas.empty()) {
-    // Earlier residue tiles of these requests ran in previous ticks.
-    if (prev) cudaStreamWaitEvent(cs, prev->done, 0);
-    rc = oz_wave_reassemble(treas, cs);
-  }
   // A tick retires only after the previous one, so completion is in order.
   if (prev) cudaStreamWaitEvent(cs, prev->done, 0);
   cudaEventRecord(slot.done, cs);
   slot.id = id;
   slot.finishing.clear();
+  slot.finishing_oz.clear();
+  slot.oz_retired = false;
   for (Req *r : touched)
     if (r->last_tick == id) {
-      slot.finishing.push_back(r->id);
+      const bool oz = r->p.tier == UVATRMM_TIER_OZAKI;
+      (oz ? slot.finishing_oz : slot.finishing).push_back(r->id);
       if (r->copy_back) {
         cudaEventCreateWithFlags(&r->d2h, cudaEventDisableTiming);
-        cudaStreamWaitEvent(s->copy, slot.done, 0);
+        cudaStreamWaitEvent(s->copy, oz ? slot.oz_done : slot.done, 0);
         cudaMemcpy2DAsync(r->p.B, r->p.ldb * 8, r->Cout, r->ldc * 8, r->t.m * 8, r->t.n, cudaMemcpyDeviceToHost,
                           s->copy);
         cudaEventRecord(r->d2h, s->copy);
@@ -543,20 +556,39 @@ void worker(uvatrmm_server_t s) {
     }
     // launch while fewer than two ticks are in flight
     if (s->inflight.size() < 2 && launch_tick(s, act)) did = true;
-    // retire the oldest tick if it finished
+    // Retire: the Ozaki requests of any tick in flight once its Ozaki work
+    // is done; the oldest tick (with its FP64 requests) once it is done.
+    auto retire = [&](const std::vector<int64_t> &ids, cudaError_t q) {
+      std::lock_guard<std::mutex> lk(s->mu);
+      for (int64_t rid : ids) {
+        Req &r = *s->reqs[rid];
+        s->active.erase(std::find(s->active.begin(), s->active.end(), rid));
+        if (r.d2h) done_wait.push_back(rid);
+        else finish(s, r, q == cudaSuccess ? r.status : UVATRMM_EDEVICE);
+      }
+      s->cv_done.notify_all();
+    };
+    for (int64_t tid : s->inflight) {
+      TickSlot &slot = s->slots[tid % uvatrmm_server_st::kSlots];
+      if (slot.oz_retired) continue;
+      const cudaError_t q = cudaEventQuery(slot.oz_done);
+      if (q == cudaErrorNotReady) continue;
+      slot.oz_retired = true;
+      if (!slot.finishing_oz.empty()) {
+        retire(slot.finishing_oz, q);
+        did = true;
+      }
+    }
     if (!s->inflight.empty()) {
       TickSlot &slot = s->slots[s->inflight.front() % uvatrmm_server_st::kSlots];
       cudaError_t q = cudaEventQuery(slot.done);
       if (q != cudaErrorNotReady) {
         s->inflight.pop_front();
-        std::lock_guard<std::mutex> lk(s->mu);
-        for (int64_t rid : slot.finishing) {
-          Req &r = *s->reqs[rid];
-          s->active.erase(std::find(s->active.begin(), s->active.end(), rid));
-          if (r.d2h) done_wait.push_back(rid);
-          else finish(s, r, q == cudaSuccess ? r.status : UVATRMM_EDEVICE);
+        if (!slot.oz_retired) {
+          slot.oz_retired = true;
+          retire(slot.finishing_oz, q);
         }
-        s->cv_done.notify_all();
+        retire(slot.finishing, q);
         did = true;
       }
     }
@@ -628,6 +660,8 @@ UVATRMM_API int uvatrmm_server_create(uvatrmm_handle_t h, const uvatrmm_server_c
     if (e == cudaSuccess) e = cudaMallocHost(&sl.host, s->slot_bytes);
     if (e == cudaSuccess) e = cudaEventCreateWithFlags(&sl.done, cudaEventDisableTiming);
     if (e == cudaSuccess) e = cudaEventCreateWithFlags(&sl.prepped, cudaEventDisableTiming);
+    if (e == cudaSuccess) e = cudaEventCreateWithFlags(&sl.gemm_done, cudaEventDisableTiming);
+    if (e == cudaSuccess) e = cudaEventCreateWithFlags(&sl.oz_done, cudaEventDisableTiming);
   }
   if (e == cudaSuccess && (fp64_group_prepare(64, UVATRMM_ENGINE_DFMA) || oz_gemm_prepare())) e = cudaErrorUnknown;
   if (e != cudaSuccess) {
@@ -780,6 +814,8 @@ UVATRMM_API int uvatrmm_server_destroy(uvatrmm_server_t s) {
     if (sl.host) cudaFreeHost(sl.host);
     if (sl.done) cudaEventDestroy(sl.done);
     if (sl.prepped) cudaEventDestroy(sl.prepped);
+    if (sl.gemm_done) cudaEventDestroy(sl.gemm_done);
+    if (sl.oz_done) cudaEventDestroy(sl.oz_done);
   }
   if (s->arena) cudaFree(s->arena);
   for (auto cs : s->cstream)
