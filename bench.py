@@ -804,8 +804,8 @@ def bf16_peak():
 def ozaki_mma_flops(m, n, moduli, side_left=True, lower=True):
     """bf16 MMA flops the residue GEMM issues for one call (tile-exact): CTA pairs
     cover 256 rows x 256 columns over one K range (for a triangular left operand,
-    the union of both 128-row tiles' ranges)."""
-    BM, BN, BK, PAIR = 128, 256, 64, 2
+    the union of both 128-row tiles' ranges), in slabs of 128."""
+    BM, BN, BK, PAIR = 128, 256, 128, 2
     Mp, Np = -(-m // (PAIR * BM)) * PAIR * BM, -(-n // BN) * BN
     K = m if side_left else n
     total = 0
