@@ -243,6 +243,11 @@ UVATRMM_API int uvatrmm_ozaki_dtrmm_device(uvatrmm_handle_t h, int layout, int s
   if (int bad = check_args(layout, side, uplo, transa, diag, m, n, lda, ldb))
     return fail(UVATRMM_EINVAL, "parameter " + std::to_string(bad) + " had an illegal value");
   const Trmm t = normalise(layout, side, uplo, transa, diag, m, n, alpha);
+  // Nothing to compare (empty, alpha = 0) or an invalid slice count: the
+  // plain path reports it before anything is copied.
+  if (t.m == 0 || t.n == 0 || alpha == 0.0 || (moduli != 0 && (moduli < 2 || moduli > kMaxModuli)))
+    return ozaki_device(h, layout, side, uplo, transa, diag, m, n, alpha, dA, lda, dB, ldb, moduli, relerr_out,
+                        bits_out);
   *relerr_out = 0.0;
   const bool left = t.side == CblasLeft;
   const int64_t len = left ? t.m : t.n, cnt = left ? t.n : t.m, ka = len;

@@ -480,7 +480,6 @@ __global__ void __launch_bounds__(Cfg<BM>::THREADS, Cfg<BM>::MIN_BLOCKS)
   uint64_t *full = reinterpret_cast<uint64_t *>(base + C::STAGES * C::STAGE_BYTES);
   uint64_t *empty = full + C::STAGES;
   StageInfo *info = reinterpret_cast<StageInfo *>(empty + C::STAGES);
-  uint64_t *never = reinterpret_cast<uint64_t *>(info + C::STAGES);  // nothing arrives on it
   auto Lst = [&](int s) { return reinterpret_cast<double *>(base + s * C::STAGE_BYTES); };
   auto Rst = [&](int s) { return reinterpret_cast<double *>(base + s * C::STAGE_BYTES) + C::L_ELEMS; };
 
@@ -490,7 +489,6 @@ __global__ void __launch_bounds__(Cfg<BM>::THREADS, Cfg<BM>::MIN_BLOCKS)
       mbar_init(&full[s], 1);
       mbar_init(&empty[s], C::NCW);
     }
-    mbar_init(never, 1);
     fence_barrier_init();
   }
   __syncthreads();
