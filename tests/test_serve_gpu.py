@@ -146,3 +146,23 @@ def test_submitters_on_several_threads(handle):
         assert srv.stats()["completed"] == len(probs)
     finally:
         srv.close()
+
+
+def test_latency_of_each_request(handle):
+    """uvatrmm_server_latency: every completed request has a submit-to-result
+    latency within the server's own bounds; an unknown id is refused."""
+    import ctypes as C
+    probs = mixed_problems(10, seed=25, max_dim=300)
+    srv = u.Server(handle, hbm_budget_bytes=1 << 30)
+    try:
+        ids = [srv.submit(p) for p in probs]
+        for rid in ids:
+            assert srv.wait(rid) == 0
+        lats = [srv.latency_ms(rid) for rid in ids]
+        st = srv.stats()
+        assert all(x is not None and 0.0 < x <= st["max_ms"] + 1e-9 for x in lats)
+        assert abs(max(lats) - st["max_ms"]) < 1e-6
+        v = C.c_double()
+        assert u.lib().uvatrmm_server_latency(srv.s, 10 ** 9, C.byref(v)) == u.EINVAL
+    finally:
+        srv.close()
