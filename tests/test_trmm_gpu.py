@@ -283,3 +283,26 @@ def test_wait_expiry_reports_etimeout_and_the_handle_recovers(handle):
             check_close(dB.cpu().numpy(), ref, B, m)
     finally:
         h.close()
+
+
+def test_allocation_failure_is_reported_and_the_next_calls_run(handle):
+    """An allocation the device cannot hold fails with UVATRMM_ENOMEM, both
+    for the library's allocator and for a server whose HBM budget exceeds the
+    device; the failure leaves nothing behind, so the next calls on the same
+    thread (a TRMM and its kernel launch) still run and are correct."""
+    import ctypes as C
+
+    import torch
+    p = C.c_void_p()
+    assert u.lib().uvatrmm_device_alloc(1 << 50, C.byref(p)) == u.ENOMEM
+    assert b"cudaMalloc" in u.lib().uvatrmm_last_error()
+    with pytest.raises(u.UvatrmmError) as ei:
+        u.Server(handle, hbm_budget_bytes=1 << 50)
+    assert ei.value.status == u.ENOMEM
+    m, n = 200, 150
+    A, lda, B, ldb = make_problem(COL, LEFT, UPPER, m, n, seed=9)
+    ref = oracle_result(COL, LEFT, UPPER, NOTRANS, NONUNIT, m, n, 1.0, A, lda, B, ldb)
+    dA, dB = torch_dev(A), torch_dev(B.copy())
+    handle.dtrmm_device(COL, LEFT, UPPER, NOTRANS, NONUNIT, m, n, 1.0, dA, lda, dB, ldb)
+    handle.sync()
+    check_close(dB.cpu().numpy(), ref, B, m)

@@ -26,6 +26,11 @@ int ok() {
   return UVATRMM_OK;
 }
 int cuda_fail(cudaError_t e, const char *what) {
+  // A failed call such as an allocation that did not fit also sets the
+  // runtime's last-error state; consume it so the check after this thread's
+  // next kernel launch does not report it a second time.  (Sticky errors,
+  // which leave the context unusable, are not cleared by this.)
+  cudaGetLastError();
   return fail(e == cudaErrorMemoryAllocation ? UVATRMM_ENOMEM : UVATRMM_EDEVICE,
               std::string(what) + ": " + cudaGetErrorString(e));
 }
