@@ -66,11 +66,15 @@ def _sig(x, d=3):
 
 
 def summary(out):
-    """Compact end of the JSON line: the checks, the Ozaki figures and the serving result."""
+    """Compact end of the JSON line: the checks, the Ozaki figures and the serving result
+    (a section that failed shows its error instead)."""
     s = {}
+    for k in ("ozaki", "variants", "serving", "next_rows", "batch"):
+        if isinstance(out.get(k), dict) and "error" in out[k]:
+            s.setdefault("errors", {})[k] = out[k]["error"][:120]
     chk = {"headline_rel_err": _sig(out.get("check", {}).get("sampled_rel_fro_err_vs_openblas"))}
     var = out.get("variants")
-    if var:
+    if var and "cases" in var:
         cases = {f'{c["uplo"]} {c["schedule/shape"]}': _sig(c.get("rel_err")) for c in var["cases"]}
         for k in ("dmma_engine", "skinny", "large"):
             if k in var:
@@ -79,7 +83,7 @@ def summary(out):
     chk["tol_8_k_eps"] = _sig(out.get("check", {}).get("tol"))
     s["check"] = chk
     oz = out.get("ozaki")
-    if oz:
+    if oz and "slice_sweep" in oz:
         s["ozaki"] = {"tflops": oz["value"], "x_plain": oz["speedup_vs_plain_fp64"], "moduli": oz["moduli"],
                       "bits": oz["bits"], "rel_err_dd": _sig(oz["rel_fro_err_vs_dd_oracle"]),
                       "lib_rel_err_host_fp64": _sig(oz.get("library_relerr_vs_host_fp64")),
@@ -88,7 +92,7 @@ def summary(out):
                       "int8_sweep": [[e.get("int8_slices"), e["moduli"], e["bits"], _sig(e["rel_fro_err_vs_dd_oracle"])]
                                      for e in oz["slice_sweep"]]}
     sv = out.get("serving")
-    if sv:
+    if sv and "rates" in sv:
         s["serving"] = {"max_steady_rate": sv["max_steady_rate_req_per_s"],
                         "max_rate_p99_2x_alone": sv.get("max_rate_p99_within_2x_alone"),
                         "alone_p99_ms": sv["alone_p99_ms"],
@@ -353,6 +357,15 @@ def run_gpu(args, ws, rank, local):
 SINGLE_GPU_SECTIONS = ("ozaki", "variants", "next_rows", "batch", "serving")
 
 
+def _guarded(fn, *a):
+    """A section's result, or its error: a failure in one diagnostic section
+    is recorded in the line instead of ending the run before the line prints."""
+    try:
+        return fn(*a)
+    except Exception as e:  # noqa: BLE001
+        return {"error": f"{type(e).__name__}: {e}"[:400]}
+
+
 def run_sections(args, ws, rank, h, dev, stream, plain_tflops, fp64_peak):
     """The sections after the headline.  They are single-GPU measurements:
     under torchrun (ws > 1) every rank runs the headline replica only and the
@@ -364,18 +377,18 @@ def run_sections(args, ws, rank, h, dev, stream, plain_tflops, fp64_peak):
                                    "why": "single-GPU sections; at N > 1 each rank runs the plain FP64 replica only"}
         return out
     if not args.no_ozaki:
-        out["ozaki"] = run_ozaki(args, h, dev, stream, rank, plain_tflops)
+        out["ozaki"] = _guarded(run_ozaki, args, h, dev, stream, rank, plain_tflops)
     if args.variants:
-        out["variants"] = run_variants(args, h, dev, stream, fp64_peak)
+        out["variants"] = _guarded(run_variants, args, h, dev, stream, fp64_peak)
     if args.next_n > 0:
-        out["next_rows"] = run_next_rows(args, h, dev, stream, fp64_peak)
+        out["next_rows"] = _guarded(run_next_rows, args, h, dev, stream, fp64_peak)
     if args.batch > 0:
         hb = u.Handle(stream=stream)  # its own workspace for the one-call-per-problem comparison
-        out["batch"] = run_batch(args, hb, dev, stream)
+        out["batch"] = _guarded(run_batch, args, hb, dev, stream)
         hb.close()
     if args.serve > 0:
         hs = u.Handle(stream=stream)
-        out["serving"] = run_serving(args, hs, dev, stream)
+        out["serving"] = _guarded(run_serving, args, hs, dev, stream)
         hs.close()
     return out
 
@@ -986,7 +999,7 @@ def main():
         torch.distributed.init_process_group("nccl")
     out = run_gpu(args, ws, rank, local)
     if rank == 0 and not args.no_cpu_baseline:
-        out["cpu_baseline"] = cpu_reference_sample(args.cpu_n, 1, 1, threads)
+        out["cpu_baseline"] = _guarded(cpu_reference_sample, args.cpu_n, 1, 1, threads)
     if rank == 0:
         out["summary"] = summary(out)
     if ws > 1:

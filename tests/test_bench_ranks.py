@@ -134,3 +134,36 @@ def test_reference_arm_reports_the_headline_config():
     import bench
     c = bench.headline_config(16384, 16384, 1)
     assert c["m"] == c["n"] == 16384 and "seed 1" in c["workload"]
+
+
+def test_a_failing_section_is_recorded_and_the_line_still_prints(monkeypatch):
+    """An exception in one diagnostic section becomes an `error` entry of that
+    section; the other sections still run and the summary names the failure."""
+    import argparse
+
+    sys.path.insert(0, ROOT)
+    import bench
+    import uvatrmm_gb300
+
+    def boom(*a, **k):
+        raise RuntimeError("device said no")
+
+    monkeypatch.setattr(bench, "run_ozaki", boom)
+    for name in ("run_variants", "run_next_rows", "run_batch", "run_serving"):
+        monkeypatch.setattr(bench, name, lambda *a, **k: {"ok": True})
+
+    class FakeHandle:
+        def __init__(self, *a, **k):
+            pass
+
+        def close(self):
+            pass
+
+    monkeypatch.setattr(uvatrmm_gb300, "Handle", FakeHandle)
+    args = argparse.Namespace(no_ozaki=False, variants=True, next_n=8, batch=5, serve=5)
+    out = bench.run_sections(args, 1, 0, None, None, None, 1.0, 1.0)
+    assert out["ozaki"] == {"error": "RuntimeError: device said no"}
+    assert out["batch"] == {"ok": True} and out["serving"] == {"ok": True}
+    s = bench.summary(dict(out, check={}))
+    assert s["errors"] == {"ozaki": "RuntimeError: device said no"}
+    json.dumps(s)
