@@ -2,7 +2,7 @@
 
 Bars: bit-exact where the exact product is representable (integer inputs);
 relative Frobenius error <= 1e-14 against the oracle's double-double TRMM
-otherwise (the spec accuracy target).
+otherwise (the accuracy target of the emulated tier).
 """
 import itertools
 
