@@ -44,14 +44,13 @@ sys.path.insert(0, ROOT)
 METRIC = "TRMM TFLOP/s, FP64 DMMA vs Ozaki at <=1e-14 rel err; served p50/p99 latency"
 NOMINAL_FP64_TFLOPS = 1.25
 FP64_FLOP_PER_CLK_SM = 4.0
-# DRAM bytes (read + write) per launch of the FP64 kernel measured by ncu on
-# smaller cases of the headline workload.  They grow faster than the flops
-# (x19.9 for x8 from 4096 to 8192: B panels are re-read per row tile and hit
-# L2 less as the operands grow), so they are not scaled to the bench size and
-# `traffic` is null there.
-TRAFFIC_MEASURED = {4096: 1.2965e9, 8192: 25.756e9}
-TRAFFIC_SOURCE = ("ncu dram__bytes_read.sum + dram__bytes_write.sum per launch at the sizes in traffic_measured; "
-                  "traffic grows faster than flops, so no figure is extrapolated to this size")
+# DRAM bytes (read + write) of one launch of the FP64 kernel (m = n, side L,
+# lower, no transpose), measured by ncu (dram__bytes_read.sum +
+# dram__bytes_write.sum, first launch, cold L2) with the banded tile order:
+# 1.73x, 4.23x and 8.67x the algorithmic bytes 8 (m(m+1)/2 + 2 m n).
+TRAFFIC_MEASURED = {4096: 0.5810e9, 8192: 5.6793e9, 16384: 46.5478e9}
+TRAFFIC_SOURCE = ("ncu --metrics dram__bytes_read.sum,dram__bytes_write.sum -k regex:trmm_fp64_kernel -c 1 "
+                  "python -m uvatrmm_gb300.run_case --tier fp64 --m M --reps 1 (one pass), per launch")
 
 
 def headline_config(m, n, ws):

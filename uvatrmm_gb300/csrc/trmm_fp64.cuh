@@ -57,7 +57,12 @@ struct TileProb {
   int tri_left, tri_lower, unit, trapezoid;
   int tri_none;                     // no triangular operand: a plain GEMM over all of K
   int n_major, n_minor, major_rev;  // tiles along the triangular dimension / the other one
+  int band;                         // minor tiles per band of the dynamic order (1..n_minor)
 };
+
+// Minor tiles per band of the dynamic tile order for a problem with inner
+// dimension K and n_minor minor tiles of edge BN.
+int fp64_dynamic_band(int64_t K, int BN, int n_minor);
 
 // One problem of a grouped launch, as the device reads it (128-byte aligned
 // like CUtensorMap: the tensor maps are read by TMA from global memory).
