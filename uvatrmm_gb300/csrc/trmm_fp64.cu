@@ -163,8 +163,17 @@ struct DfmaEngine {
   using C = Cfg<BM>;
   double acc[C::TM][C::TN];
   int tx, ty;
+  int nii, njj;  // register-row blocks / column blocks of this warp inside the tile's valid part
 
   __device__ void init(int tid) { tx = tid & 15; ty = tid >> 4; }
+  // Valid part of the current tile (rows x cols of BM x BN).  A warp owns
+  // rows tw + TY*ii and tw + 1 + TY*ii (tw = ty & ~1) and every column block,
+  // so both counts are the same in all its lanes.
+  __device__ void extent(int rows, int cols) {
+    const int tw = ty & ~1;
+    nii = rows > tw ? min(C::TM, (rows - tw + C::TY - 1) / C::TY) : 0;
+    njj = min(C::TN, (cols + 15) / 16);
+  }
   __device__ void zero() {
 #pragma unroll
     for (int ii = 0; ii < C::TM; ++ii)
@@ -186,45 +195,94 @@ struct DfmaEngine {
       }
     }
   }
+  // Part of a slab: register rows [LO, HI) only and column blocks below
+  // njj; with SEL, a diagonal slab (k in [c0, c0 + 16) of the tile's
+  // diagonal block) whose triangle lies on the left operand.  Rows left out
+  // never issue their FMAs: a predicated-off DFMA still holds the FP64 pipe
+  // (measured: per-lane skip predicates saved no time), so the row range is
+  // a template argument and the column blocks are left by a branch.
+  template <bool LK, bool RK, int LO, int HI, bool SEL>
+  __device__ void part(const double *Ls, const double *Rs, int c0, bool lower, bool unit) {
+#pragma unroll 1
+    for (int k = 0; k < kBK; ++k) {
+      double a[C::TM];
+#pragma unroll
+      for (int ii = LO; ii < HI; ++ii) {
+        const int r = ty + C::TY * ii;
+        a[ii] = ldL<BM, LK>(Ls, r, k);
+        if (SEL) a[ii] = tri_select(a[ii], tri_class(r, c0 + k, lower), unit);
+      }
+#pragma unroll
+      for (int jj = 0; jj < C::TN; ++jj) {
+        if (jj >= njj) break;
+        const double b = ldR<C::BN, RK>(Rs, k, tx + 16 * jj);
+#pragma unroll
+        for (int ii = LO; ii < HI; ++ii) acc[ii][jj] = fma(a[ii], b, acc[ii][jj]);
+      }
+    }
+  }
+  template <bool LK, bool RK, bool SEL>
+  __device__ void part_rows(const double *Ls, const double *Rs, int lo, int hi, int c0, bool lower, bool unit) {
+    static_assert(C::TM == 4, "row-range dispatch covers four register rows");
+    switch (lo * 8 + hi) {
+#define UVT_PART(L, H) \
+  case L * 8 + H: part<LK, RK, L, H, SEL>(Ls, Rs, c0, lower, unit); break;
+      UVT_PART(0, 1) UVT_PART(0, 2) UVT_PART(0, 3) UVT_PART(0, 4)
+      UVT_PART(1, 2) UVT_PART(1, 3) UVT_PART(1, 4)
+      UVT_PART(2, 3) UVT_PART(2, 4)
+      UVT_PART(3, 4)
+#undef UVT_PART
+      default: break;  // no rows of this warp hold work in this slab
+    }
+  }
+  // A slab of a tile that overhangs the matrix: only the register rows and
+  // column blocks that hold valid outputs are computed (the others would
+  // only multiply the zero fill of the out-of-range TMA boxes).
+  template <bool LK, bool RK>
+  __device__ void slab_edge(const double *Ls, const double *Rs) {
+    part_rows<LK, RK, false>(Ls, Rs, 0, nii, 0, false, false);
+  }
   // Diagonal slab `s` (k in [16s, 16s+16) of the tile's diagonal block,
   // whose rows and columns share the same origin).
   template <bool LK, bool RK>
   __device__ void slab_diag(const double *Ls, const double *Rs, int s, const TileProb &p) {
     const bool trap = p.trapezoid, lower = p.tri_lower, unit = p.unit;
     const int c0 = 16 * s;
+    if (!p.tri_left) {
 #pragma unroll 1
-    for (int k = 0; k < kBK; ++k) {
-      double a[C::TM];
-      bool skip[C::TM];
+      for (int k = 0; k < kBK; ++k) {
+        double a[C::TM];
 #pragma unroll
-      for (int ii = 0; ii < C::TM; ++ii) {
-        a[ii] = ldL<BM, LK>(Ls, ty + C::TY * ii, k);
-        skip[ii] = false;
-      }
-      if (p.tri_left) {
-        // op(A)[r, c0 + k] with r = ty + TY*ii; rows wholly above (lower)
-        // or below (upper) the slab lie outside the trapezoid.
+        for (int ii = 0; ii < C::TM; ++ii) a[ii] = ldL<BM, LK>(Ls, ty + C::TY * ii, k);
 #pragma unroll
-        for (int ii = 0; ii < C::TM; ++ii) {
-          const int r = ty + C::TY * ii;
-          a[ii] = tri_select(a[ii], tri_class(r, c0 + k, lower), unit);
-          skip[ii] = trap && (lower ? (r < c0) : (r > c0 + kBK - 1));
-        }
-      }
-#pragma unroll
-      for (int jj = 0; jj < C::TN; ++jj) {
-        double b = ldR<C::BN, RK>(Rs, k, tx + 16 * jj);
-        if (!p.tri_left) {
-          // op(A)[c0 + k, c] with c = tx + 16*jj.
+        for (int jj = 0; jj < C::TN; ++jj) {
+          if (jj >= njj) break;
+          // op(A)[c0 + k, c] with c = tx + 16*jj; with TRAPEZOID, column
+          // blocks wholly right (lower) or left (upper) of the slab are
+          // skipped (the same in all lanes: c0 is a multiple of 16).
           const int c = tx + 16 * jj;
-          b = tri_select(b, tri_class(c0 + k, c, lower), unit);
+          const double b = tri_select(ldR<C::BN, RK>(Rs, k, c), tri_class(c0 + k, c, lower), unit);
           if (trap && (lower ? (c > c0 + kBK - 1) : (c < c0))) continue;
-        }
 #pragma unroll
-        for (int ii = 0; ii < C::TM; ++ii)
-          if (!skip[ii]) acc[ii][jj] = fma(a[ii], b, acc[ii][jj]);
+          for (int ii = 0; ii < C::TM; ++ii) {
+            if (ii >= nii) break;
+            acc[ii][jj] = fma(a[ii], b, acc[ii][jj]);
+          }
+        }
       }
+      return;
     }
+    // op(A)[r, c0 + k] with r = ty + TY*ii.  With TRAPEZOID, register rows
+    // wholly above (lower) or below (upper) the slab are skipped; a warp's
+    // two rows tw, tw + 1 (tw even, c0 a multiple of 16) always fall on the
+    // same side, so the row range is the same in all its lanes.
+    const int tw = ty & ~1;
+    int lo = 0, hi = nii;
+    if (trap) {
+      if (lower) lo = c0 - tw - 1 > 0 ? (c0 - tw - 1 + C::TY - 1) / C::TY : 0;
+      else hi = c0 + kBK - 1 - tw < 0 ? 0 : min(hi, (c0 + kBK - 1 - tw) / C::TY + 1);
+    }
+    part_rows<LK, RK, true>(Ls, Rs, lo, hi, c0, lower, unit);
   }
   __device__ void store(const TileProb &p, int64_t i0, int64_t j0) {
 #pragma unroll
@@ -263,6 +321,10 @@ struct DmmaEngine {
     g = lane >> 2;
     t = lane & 3;
   }
+  // The DMMA engine computes whole tiles (fragments span 8 rows and columns).
+  __device__ void extent(int, int) {}
+  template <bool LK, bool RK>
+  __device__ void slab_edge(const double *Ls, const double *Rs) { slab<LK, RK>(Ls, Rs); }
   __device__ void zero() {
 #pragma unroll
     for (int f = 0; f < FM; ++f)
@@ -447,12 +509,18 @@ __global__ void __launch_bounds__(Cfg<BM>::THREADS, Cfg<BM>::MIN_BLOCKS)
       const volatile StageInfo *vi = &info[s];
       const StageInfo inf{vi->ti, vi->tj, vi->kt, vi->flags};
       if (inf.ti < 0) break;
-      if (inf.flags & SF_FIRST) eng.zero();
       const int64_t i0 = (int64_t)inf.ti * BM, j0 = (int64_t)inf.tj * C::BN;
+      const bool edge = i0 + BM > p.M || j0 + C::BN > p.N;
+      if (inf.flags & SF_FIRST) {
+        eng.zero();
+        eng.extent((int)min((int64_t)BM, p.M - i0), (int)min((int64_t)C::BN, p.N - j0));
+      }
       const int64_t k0 = (int64_t)inf.kt * kBK;
       const int64_t d0 = p.tri_left ? i0 : j0;
       if (!p.tri_none && k0 >= d0 && k0 < d0 + BM)
         eng.template slab_diag<LK, RK>(Lst(s), Rst(s), (int)((k0 - d0) / kBK), p);
+      else if (edge)
+        eng.template slab_edge<LK, RK>(Lst(s), Rst(s));
       else
         eng.template slab<LK, RK>(Lst(s), Rst(s));
       __syncwarp();
@@ -572,8 +640,12 @@ __global__ void __launch_bounds__(Cfg<BM>::THREADS, Cfg<BM>::MIN_BLOCKS)
       if (inf.ti < 0) break;
       const Fp64GroupProb &P = probs[inf.prob];
       const TileProb tp = P.tp;
-      if (inf.flags & SF_FIRST) eng.zero();
       const int64_t i0 = (int64_t)inf.ti * BM, j0 = (int64_t)inf.tj * C::BN;
+      const bool edge = i0 + BM > tp.M || j0 + C::BN > tp.N;
+      if (inf.flags & SF_FIRST) {
+        eng.zero();
+        eng.extent((int)min((int64_t)BM, tp.M - i0), (int)min((int64_t)C::BN, tp.N - j0));
+      }
       const int64_t k0 = (int64_t)inf.kt * kBK;
       const int64_t d0 = tp.tri_left ? i0 : j0;
       const double *Ls = Lst(s), *Rs = Rst(s);
@@ -585,6 +657,13 @@ __global__ void __launch_bounds__(Cfg<BM>::THREADS, Cfg<BM>::MIN_BLOCKS)
           case 2: eng.template slab_diag<true, false>(Ls, Rs, sd, tp); break;
           case 1: eng.template slab_diag<false, true>(Ls, Rs, sd, tp); break;
           default: eng.template slab_diag<false, false>(Ls, Rs, sd, tp); break;
+        }
+      } else if (edge) {
+        switch (lay) {
+          case 3: eng.template slab_edge<true, true>(Ls, Rs); break;
+          case 2: eng.template slab_edge<true, false>(Ls, Rs); break;
+          case 1: eng.template slab_edge<false, true>(Ls, Rs); break;
+          default: eng.template slab_edge<false, false>(Ls, Rs); break;
         }
       } else {
         switch (lay) {
