@@ -76,6 +76,30 @@ def test_schedules_shapes_tiles(handle, tile, schedule, shape):
         handle.set_option("shape", u.SHAPE_TRAPEZOID)
 
 
+@pytest.mark.parametrize("tile", [64, 128])
+@pytest.mark.parametrize("shape", [u.SHAPE_TRAPEZOID, u.SHAPE_BOXES])
+def test_partial_and_diagonal_tiles_every_variant(handle, tile, shape):
+    """Tiles that overhang the matrix compute only their valid register rows
+    and column blocks, and trapezoid diagonal slabs skip the rows or column
+    blocks in the zero half: sizes that leave every row-range case of the
+    skipping (partial last tiles of 1-63 rows, triangles of 1-3 tiles) for
+    all 16 column-major variants, NaN in the unreferenced triangle."""
+    handle.set_option("tile", tile)
+    handle.set_option("shape", shape)
+    try:
+        for side, uplo, trans, diag in itertools.product((LEFT, RIGHT), (LOWER, UPPER), (NOTRANS, TRANS),
+                                                         (NONUNIT, UNIT)):
+            for (m, n) in ((50, 33), (111, 70), (200, 17), (18, 145)):
+                A, lda, B, ldb = make_problem(COL, side, uplo, m, n, ldb_pad=2)
+                ref = oracle_result(COL, side, uplo, trans, diag, m, n, -1.5, A, lda, B, ldb)
+                got = B.copy()
+                handle.dtrmm(COL, side, uplo, trans, diag, m, n, -1.5, A, lda, got, ldb)
+                check_close(got, ref, B, m if side == LEFT else n)
+    finally:
+        handle.set_option("tile", 0)
+        handle.set_option("shape", u.SHAPE_TRAPEZOID)
+
+
 @pytest.mark.parametrize("m,n", [(0, 5), (5, 0), (1, 1), (1, 17), (17, 1), (2, 3), (63, 65), (129, 2)])
 def test_edge_sizes(handle, m, n):
     for side in (LEFT, RIGHT):
