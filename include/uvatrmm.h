@@ -106,7 +106,8 @@ typedef enum {
                                        plain FP64 kernel on the device */
 } uvatrmm_option;
 typedef enum { UVATRMM_ENGINE_DFMA = 0, UVATRMM_ENGINE_DMMA = 1 } uvatrmm_engine;
-/* DYNAMIC: persistent CTAs pull tiles in longest-first order.
+/* DYNAMIC: persistent CTAs pull tiles from a counter, in bands of 1024
+ * columns of the non-triangular operand, longest row tiles first in a band.
  * REG / BALANCED: the reference's row mappings (map_regular / map_balanced)
  * applied to row tiles; each CTA owns one row block x one column panel. */
 typedef enum { UVATRMM_SCHED_DYNAMIC = 0, UVATRMM_SCHED_REG = 1, UVATRMM_SCHED_BALANCED = 2 } uvatrmm_schedule;

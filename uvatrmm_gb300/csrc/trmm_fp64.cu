@@ -535,7 +535,8 @@ __global__ void __launch_bounds__(Cfg<BM>::THREADS, Cfg<BM>::MIN_BLOCKS)
 // ---------------------------------------------------------------- grouped kernel
 // Many TRMMs in one persistent launch: the problems' tiles form one list
 // (problem p owns tiles [tile_begin, tile_begin + tile_count)), pulled from
-// an atomic counter; inside a problem, longest tiles first.  Each problem
+// an atomic counter; inside a problem, in the dynamic order of the
+// single-problem kernel (bands, longest tiles first in a band).  Each problem
 // carries its own tensor maps (in global memory) and slab layouts, which
 // the consumers dispatch on at run time.
 __device__ __forceinline__ void tmap_acquire(const CUtensorMap *m) {
