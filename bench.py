@@ -295,7 +295,9 @@ def run_gpu(args, ws, rank, local):
     # Pipelined: a stream of independent products through uvatrmm_dtrmm_async
     # on two handles (double-buffered B), so one step's copies overlap the
     # other's product; every step still copies its A and B in and B out.
-    h2 = u.Handle()
+    # The second handle gets its own non-blocking stream: on the legacy default
+    # stream the same loop ran 1.1 % slower (36.37 against 35.96 s for 10 steps).
+    h2 = u.Handle(stream=torch.cuda.Stream(dev))
     hs = [h, h2]
     for hh, b in zip(hs, hBs):  # warm-up (allocates each handle's workspace)
         hh.dtrmm_async(L, u.LEFT, Lo, NT, NU, m, n, 1.0, hA, m, b, m)
