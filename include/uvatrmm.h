@@ -129,8 +129,9 @@ UVATRMM_API int uvatrmm_dtrmm(uvatrmm_handle_t handle, int layout, int side, int
  * handle's stream, and returns.  A and B must lie in uvatrmm_host_alloc
  * memory (else UVATRMM_EINVAL) and stay untouched until uvatrmm_sync(handle),
  * which waits and reports the kernel status.  Calls on one handle run in
- * order; calls on two handles overlap one problem's copies with the other's
- * product. */
+ * order; calls on two handles whose streams are distinct non-blocking
+ * streams (uvatrmm_set_stream; a new handle uses the legacy default stream)
+ * overlap one problem's copies with the other's product. */
 UVATRMM_API int uvatrmm_dtrmm_async(uvatrmm_handle_t handle, int layout, int side, int uplo, int transa, int diag,
                                     int64_t m, int64_t n, double alpha, const double *A, int64_t lda, double *B,
                                     int64_t ldb);
