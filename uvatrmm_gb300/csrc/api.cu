@@ -249,7 +249,7 @@ int host_trmm(uvatrmm_handle_t h, int layout, int side, int uplo, int transa, in
   double *dB = static_cast<double *>(workspace(h, 1, (size_t)lb * t.n * 8));
   double *dC = static_cast<double *>(workspace(h, 2, (size_t)lb * t.n * 8));
   if (!dA || !dB || !dC) return tl_status;
-  cudaError_t e = host_copy2d(h, dA, la * 8, A, lda * 8, ka * 8, ka, cudaMemcpyHostToDevice);
+  cudaError_t e = copy_triangle_h2d(h, dA, la, A, lda, ka, t.uplo == CblasLower);
   if (e == cudaSuccess) e = host_copy2d(h, dB, lb * 8, B, ldb * 8, t.m * 8, t.n, cudaMemcpyHostToDevice);
   if (e != cudaSuccess) return cuda_fail(e, "host to device copy");
   int rc = run_fp64(h, t, dA, la, dB, lb, dC, lb, h->schedule, h->shape);

@@ -69,6 +69,14 @@ void *workspace(uvatrmm_handle_t h, int slot, size_t bytes);
 // runs.  A device-to-host copy has landed in `dst` when this returns.
 cudaError_t host_copy2d(uvatrmm_handle_t h, void *dst, size_t dpitch, const void *src, size_t spitch, size_t width,
                         size_t height, cudaMemcpyKind kind);
+// Host-to-device copy of the referenced triangle of the ka x ka
+// column-major A (lower: rows j..ka-1 of column j; upper: rows 0..j), in
+// blocks of kTriCopyCols columns, each block the rectangle over its part of
+// the triangle.  The device copy's other entries are left as they were: the
+// kernels never use the unreferenced triangle's values.
+constexpr int64_t kTriCopyCols = 256;
+cudaError_t copy_triangle_h2d(uvatrmm_handle_t h, double *dA, int64_t la, const double *A, int64_t lda, int64_t ka,
+                              bool lower);
 // True when [p, p + bytes) lies inside one uvatrmm_host_alloc region.
 bool host_alloc_contains(const void *p, size_t bytes);
 // Frees the handle's staging buffers and events.

@@ -119,6 +119,18 @@ void par_copy(void *dst, size_t dpitch, const void *src, size_t spitch, size_t w
 
 bool host_alloc_contains(const void *p, size_t bytes) { return in_host_alloc(p, bytes); }
 
+cudaError_t copy_triangle_h2d(uvatrmm_handle_t h, double *dA, int64_t la, const double *A, int64_t lda, int64_t ka,
+                              bool lower) {
+  for (int64_t j0 = 0; j0 < ka; j0 += kTriCopyCols) {
+    const int64_t w = std::min<int64_t>(kTriCopyCols, ka - j0);
+    const int64_t r0 = lower ? j0 : 0, r1 = lower ? ka : j0 + w;
+    const cudaError_t e = host_copy2d(h, dA + r0 + j0 * la, (size_t)la * 8, A + r0 + j0 * lda, (size_t)lda * 8,
+                                      (size_t)(r1 - r0) * 8, (size_t)w, cudaMemcpyHostToDevice);
+    if (e != cudaSuccess) return e;
+  }
+  return cudaSuccess;
+}
+
 cudaError_t host_copy2d(uvatrmm_handle_t h, void *dst, size_t dpitch, const void *src, size_t spitch, size_t width,
                         size_t height, cudaMemcpyKind kind) {
   if (width == 0 || height == 0) return cudaSuccess;

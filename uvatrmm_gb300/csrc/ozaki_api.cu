@@ -284,7 +284,7 @@ UVATRMM_API int uvatrmm_ozaki_dtrmm(uvatrmm_handle_t h, int layout, int side, in
   double *dA = static_cast<double *>(workspace(h, 0, (size_t)la * ka * 8));
   double *dB = static_cast<double *>(workspace(h, 2, (size_t)lb * t.n * 8));
   if (!dA || !dB) return uvatrmm_last_status();
-  cudaError_t e = host_copy2d(h, dA, la * 8, A, lda * 8, ka * 8, ka, cudaMemcpyHostToDevice);
+  cudaError_t e = copy_triangle_h2d(h, dA, la, A, lda, ka, t.uplo == CblasLower);
   if (e == cudaSuccess) e = host_copy2d(h, dB, lb * 8, B, ldb * 8, t.m * 8, t.n, cudaMemcpyHostToDevice);
   if (e != cudaSuccess) return cuda_fail(e, "host to device copy");
   // Error report: the sampled inputs are kept before B is overwritten; the
