@@ -76,14 +76,17 @@ def test_schedules_shapes_tiles(handle, tile, schedule, shape):
         handle.set_option("shape", u.SHAPE_TRAPEZOID)
 
 
+@pytest.mark.parametrize("engine", [u.ENGINE_DFMA, u.ENGINE_DMMA])
 @pytest.mark.parametrize("tile", [64, 128])
 @pytest.mark.parametrize("shape", [u.SHAPE_TRAPEZOID, u.SHAPE_BOXES])
-def test_partial_and_diagonal_tiles_every_variant(handle, tile, shape):
+def test_partial_and_diagonal_tiles_every_variant(handle, engine, tile, shape):
     """Tiles that overhang the matrix compute only their valid register rows
-    and column blocks, and trapezoid diagonal slabs skip the rows or column
-    blocks in the zero half: sizes that leave every row-range case of the
-    skipping (partial last tiles of 1-63 rows, triangles of 1-3 tiles) for
-    all 16 column-major variants, NaN in the unreferenced triangle."""
+    (DFMA) or fragments (DMMA) and column blocks, and trapezoid diagonal
+    slabs skip the rows or column blocks in the zero half: sizes that leave
+    every row-range case of the skipping (partial last tiles of 1-63 rows,
+    triangles of 1-3 tiles) for all 16 column-major variants, NaN in the
+    unreferenced triangle."""
+    handle.set_option("engine", engine)
     handle.set_option("tile", tile)
     handle.set_option("shape", shape)
     try:
@@ -96,6 +99,7 @@ def test_partial_and_diagonal_tiles_every_variant(handle, tile, shape):
                 handle.dtrmm(COL, side, uplo, trans, diag, m, n, -1.5, A, lda, got, ldb)
                 check_close(got, ref, B, m if side == LEFT else n)
     finally:
+        handle.set_option("engine", u.ENGINE_DFMA)
         handle.set_option("tile", 0)
         handle.set_option("shape", u.SHAPE_TRAPEZOID)
 

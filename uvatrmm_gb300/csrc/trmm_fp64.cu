@@ -313,6 +313,7 @@ struct DmmaEngine {
   static constexpr int FM = WM / 8, FN = WN / 8;
   double acc[FM][FN][2];
   int r0, c0, g, t;
+  int nf, nh;  // row / column fragments of this warp inside the tile's valid part
 
   __device__ void init(int tid) {
     int w = tid >> 5, lane = tid & 31;
@@ -321,10 +322,45 @@ struct DmmaEngine {
     g = lane >> 2;
     t = lane & 3;
   }
-  // The DMMA engine computes whole tiles (fragments span 8 rows and columns).
-  __device__ void extent(int, int) {}
+  // Valid part of the current tile; a fragment is a warp's, so both counts
+  // are the same in all its lanes.
+  __device__ void extent(int rows, int cols) {
+    nf = rows > r0 ? min(FM, (rows - r0 + 7) / 8) : 0;
+    nh = cols > c0 ? min(FN, (cols - c0 + 7) / 8) : 0;
+  }
+  // Fragments [0, NF) x [0, NH) of a slab: the fragment counts are template
+  // arguments, so the MMAs of fragments outside the matrix are never issued.
+  template <bool LK, bool RK, int NF, int NH>
+  __device__ void part(const double *Ls, const double *Rs) {
+#pragma unroll 1
+    for (int k = 0; k < kBK; k += 4) {
+      double a[FM], b[FN];
+#pragma unroll
+      for (int f = 0; f < NF; ++f) a[f] = ldL<BM, LK>(Ls, r0 + 8 * f + g, k + t);
+#pragma unroll
+      for (int h = 0; h < NH; ++h) b[h] = ldR<C::BN, RK>(Rs, k + t, c0 + 8 * h + g);
+#pragma unroll
+      for (int f = 0; f < NF; ++f)
+#pragma unroll
+        for (int h = 0; h < NH; ++h) dmma884(acc[f][h][0], acc[f][h][1], a[f], b[h]);
+    }
+  }
   template <bool LK, bool RK>
-  __device__ void slab_edge(const double *Ls, const double *Rs) { slab<LK, RK>(Ls, Rs); }
+  __device__ void slab_edge(const double *Ls, const double *Rs) {
+    static_assert(FM <= 4 && FN <= 4, "fragment-count dispatch covers up to four fragments each way");
+    switch (nf * 8 + nh) {
+#define UVT_FRAGS(F, H)                                             \
+  case F * 8 + H:                                                   \
+    if constexpr (F <= FM && H <= FN) part<LK, RK, F, H>(Ls, Rs); \
+    break;
+      UVT_FRAGS(1, 1) UVT_FRAGS(1, 2) UVT_FRAGS(1, 3) UVT_FRAGS(1, 4)
+      UVT_FRAGS(2, 1) UVT_FRAGS(2, 2) UVT_FRAGS(2, 3) UVT_FRAGS(2, 4)
+      UVT_FRAGS(3, 1) UVT_FRAGS(3, 2) UVT_FRAGS(3, 3) UVT_FRAGS(3, 4)
+      UVT_FRAGS(4, 1) UVT_FRAGS(4, 2) UVT_FRAGS(4, 3) UVT_FRAGS(4, 4)
+#undef UVT_FRAGS
+      default: break;  // no fragment of this warp inside the matrix
+    }
+  }
   __device__ void zero() {
 #pragma unroll
     for (int f = 0; f < FM; ++f)
@@ -362,20 +398,28 @@ struct DmmaEngine {
         for (int f = 0; f < FM; ++f) a[f] = tri_select(a[f], tri_class(r0 + 8 * f + g, kk + t, lower), unit);
 #pragma unroll
         for (int f = 0; f < FM; ++f) {
+          if (f >= nf) break;
           const int rb = r0 + 8 * f;  // fragment rows [rb, rb+8), k columns [kk, kk+4)
           if (trap && (lower ? (kk > rb + 7) : (kk + 3 < rb))) continue;
 #pragma unroll
-          for (int h = 0; h < FN; ++h) dmma884(acc[f][h][0], acc[f][h][1], a[f], b[h]);
+          for (int h = 0; h < FN; ++h) {
+            if (h >= nh) break;
+            dmma884(acc[f][h][0], acc[f][h][1], a[f], b[h]);
+          }
         }
       } else {
 #pragma unroll
         for (int h = 0; h < FN; ++h) b[h] = tri_select(b[h], tri_class(kk + t, c0 + 8 * h + g, lower), unit);
 #pragma unroll
         for (int h = 0; h < FN; ++h) {
+          if (h >= nh) break;
           const int cb = c0 + 8 * h;  // fragment columns [cb, cb+8)
           if (trap && (lower ? (kk + 3 < cb) : (kk > cb + 7))) continue;
 #pragma unroll
-          for (int f = 0; f < FM; ++f) dmma884(acc[f][h][0], acc[f][h][1], a[f], b[h]);
+          for (int f = 0; f < FM; ++f) {
+            if (f >= nf) break;
+            dmma884(acc[f][h][0], acc[f][h][1], a[f], b[h]);
+          }
         }
       }
     }
